@@ -1,0 +1,343 @@
+"""Benchmark: batched, checkpointed 3D FMC L2 gradient on one GB300.
+
+Workload (N=1): the 192^3 cylinder acquisition (dx = 0.2 mm, 8 rings x 32
+elements = 256 shots, nt = 2000, 1 MHz Ricker, seeded Gaussian random-field
+model) -- the gradient configuration the headline metric is quoted on.  One
+step = the exact discrete-adjoint L2 gradient of one batch of 32 shots (one
+ring): forward sweep with checkpoints every k steps, residual, backward sweep
+with bit-identical segment recompute and the fused imaging condition, all 32
+shots advancing in one launch per time step.  Inputs are larger than L2 (every
+launch streams ~0.9 GB per wavefield level).
+
+Reported alongside: the kernel roofline of the dominant kernel (the forward
+stencil, timed live with CUDA events on its stream), the end-to-end rate
+through the public backend API with host buffers, the plain one-shot-per-launch
+GPU form on the same workload, the reference scheme on the host cores (the
+oracle's FP64 restatement, bit-identical to the reference C++ core), SM clocks
+sampled during the timed region and the number of kernels launched.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+
+METRIC = "Grad shots/s + p50/p99, batched serve vs per-shot plain, same GB300, relerr≤1e-4"
+WORKLOAD = ("3D acoustic cylinder FMC L2 gradient, 192^3, dx=0.2mm, 8x32 elements (256 shots), "
+            "nt=2000, FP32, 32 shots per launch, checkpoint every 64 steps")
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock / throttle reasons during a region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+                for nm, v in zip(names, f[3:7]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_gradient_sample(prob, shot, nt_sample, k):
+    """Time the FP64 oracle gradient for one shot over nt_sample levels and
+    scale to the full time axis: returns (shots/s, seconds, description)."""
+    import numpy as np
+    import oracle
+    wav = prob.wavelet[:nt_sample]
+    geom = prob.geom
+    rec_all = oracle.forward_fmc(prob.m_true, geom, wav, prob.dt, prob.h, nt_sample, None, [shot])
+    t0 = time.perf_counter()
+    oracle.misfit_and_gradient(prob.m0, geom, wav, prob.dt, prob.h, nt_sample, rec_all, None,
+                               [shot], k=k)
+    dt_s = time.perf_counter() - t0
+    per_shot = dt_s * (prob.nt - 1) / (nt_sample - 1)
+    return 1.0 / per_shot, dt_s, (f"1 shot x {nt_sample} levels of the {prob.shape[0]}^3 "
+                                  f"gradient (checkpoint k={k}), scaled by (nt-1)/{nt_sample - 1}")
+
+
+def run_reference(args, prob):
+    """--impl reference: the reference scheme's CPU path on the host cores."""
+    import oracle
+    oracle.build()
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    kind = "port"
+    nt_sample = 24
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, secs, desc = cpu_gradient_sample(prob, i % prob.n_shots, nt_sample, 8)
+        if i >= args.warmup:
+            vals.append((v, secs))
+    value = statistics.median(v for v, _ in vals)
+    ms = 1000.0 / value
+    line = {"metric": METRIC, "value": value, "unit": "shots/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": value, "unit": "shots/s", "cores": cores, "kind": kind,
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "shots/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=192, help="grid size (default: the benchmark's 192)")
+    ap.add_argument("--nt", type=int, default=2000)
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--ckpt", type=int, default=64)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    import numpy as np
+    from openusct_gb300 import problems
+
+    per_ring = 32
+    prob = problems.cylinder3d(seed=0, n=args.n, h=0.2e-3 * 191 / (args.n - 1), nt=args.nt,
+                               per_ring=per_ring)
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, prob)
+        return
+
+    import torch
+    import torch.distributed as dist
+    if world > 1:
+        dist.init_process_group("nccl")
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from openusct_gb300 import _lib, backend
+    from openusct_gb300.geometry import element_csr
+    import ctypes
+
+    C = args.batch
+    # replicas: rank r owns the batches r, r+world, ...
+    shots = list(range(C * rank, C * rank + C))
+    tx, rx = element_csr(prob.geom, prob.shape, shots, None)
+    plan = backend.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx, rx, batch=C, ckpt_k=args.ckpt)
+    lib = _lib.load()
+    s = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    m_true = torch.from_numpy(prob.m_true).to(dev)
+    m0 = torch.from_numpy(prob.m0).to(dev)
+    wav = torch.from_numpy(prob.wavelet).to(dev)
+    mws = torch.empty(plan.model_bytes(), dtype=torch.uint8, device=dev)
+    bws = torch.empty(plan.batch_bytes(_lib.MODE_GRADIENT), dtype=torch.uint8, device=dev)
+    dobs = torch.empty((C, prob.nt, plan.n_rx), dtype=torch.float32, device=dev)
+    # observed data from the true model (same engine, forward only)
+    _lib.check(lib.usct_forward_fmc_dev(plan.handle, P(m_true), None, P(wav), P(dobs), P(mws),
+                                        P(bws), sp))
+    J = torch.zeros(C, dtype=torch.float64, device=dev)
+    g = torch.empty(prob.shape, dtype=torch.float64, device=dev)
+
+    def step():
+        _lib.check(lib.usct_misfit_and_gradient_dev(plan.handle, P(m0), None, P(wav), P(dobs),
+                                                    P(J), P(g), P(mws), P(bws), sp))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    launches0 = plan.info("launches")
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(s)
+        for _ in range(args.steps):
+            step()
+        ev1.record(s)
+        torch.cuda.synchronize()
+    launches = plan.info("launches") - launches0
+    t_ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        tt = torch.tensor([t_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    value = C * world / (t_ms / 1000.0)
+    cells = int(np.prod(prob.shape))
+    hbm, peak_kind = _peaks()
+    pipeline_bytes = (44 * C + 20) * cells * (prob.nt - 1)
+
+    # dominant kernel: the forward stencil launch, timed live (forward-only sweep)
+    fws = bws
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    _lib.check(lib.usct_model_prepare(plan.handle, P(mws), P(m0), None, None, P(wav), sp))
+    nrep = 2
+    e0.record(s)
+    for _ in range(nrep):
+        _lib.check(lib.usct_batch_forward(plan.handle, P(mws), P(fws), 0, _lib.MODE_FORWARD,
+                                          None, sp))
+    e1.record(s)
+    torch.cuda.synchronize()
+    t_launch = e0.elapsed_time(e1) / 1000.0 / (nrep * (prob.nt - 1))
+    fwd_bytes = (12 * C + 4) * cells
+    achieved = fwd_bytes / t_launch / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "k_forward_traffic.json")
+    if os.path.exists(prof):
+        try:
+            with open(prof) as f:
+                pj = json.load(f)
+            traffic = float(pj["dram_bytes_per_launch"]) * (cells * C) / float(pj["cell_channels"])
+        except Exception:
+            traffic = None
+
+    # end to end through the public API with host buffers (it allocates its own
+    # workspace, so release the timed one first)
+    del bws, fws
+    torch.cuda.empty_cache()
+    e2e = None
+    if rank == 0:
+        m0_h = prob.m0
+        dobs_h = dobs.double().cpu().numpy()
+        t0 = time.perf_counter()
+        ne = 1
+        for _ in range(ne):
+            Jh, gh = backend.misfit_and_gradient(m0_h, prob.geom, prob.wavelet, prob.dt, prob.h,
+                                                 prob.nt, dobs_h, src_list=shots, batch=C,
+                                                 ckpt_k=args.ckpt)
+        te = (time.perf_counter() - t0) / ne
+        e2e = {"value": C / te, "unit": "shots/s",
+               "h2d_bytes_per_step": int(m0_h.nbytes + C * prob.nt * plan.n_rx * 4 +
+                                         prob.wavelet.nbytes),
+               "d2h_bytes_per_step": int(gh.nbytes + 8 * C)}
+
+    # plain one-shot-per-launch GPU form, same workload, one shot
+    plain = None
+    if rank == 0 and not args.no_plain:
+        backend._PLANS.clear()
+        torch.cuda.empty_cache()
+        tx1, rx1 = element_csr(prob.geom, prob.shape, [0], None)
+        pplan = backend.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx1, rx1, batch=1)
+        pws = torch.empty(pplan.plain_bytes(True), dtype=torch.uint8, device=dev)
+        J1 = torch.zeros(1, dtype=torch.float64, device=dev)
+        d1 = dobs[0:1].contiguous()
+        args_p = (pplan.handle, P(m0), P(wav), P(d1), P(J1), P(g), P(pws), sp)
+        _lib.check(lib.usct_plain_misfit_and_gradient_dev(*args_p))
+        torch.cuda.synchronize()
+        e0.record(s)
+        _lib.check(lib.usct_plain_misfit_and_gradient_dev(*args_p))
+        e1.record(s)
+        torch.cuda.synchronize()
+        tp = e0.elapsed_time(e1) / 1000.0
+        plain = {"value": 1.0 / tp, "unit": "shots/s", "ms_per_shot": tp * 1000.0,
+                 "speedup_batched_vs_plain": value / world / (1.0 / tp)}
+        del pws
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            import oracle
+            oracle.build()
+            v, secs, desc = cpu_gradient_sample(prob, 0, 40, 8)
+            cpu = {"value": v, "unit": "shots/s",
+                   "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+                   "kind": "port", "sample": desc, "seconds": secs}
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "error": str(exc)[:200]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "shots/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Gaussian random-field model)",
+            "config": {"workload": WORKLOAD if args.n == 192 and args.nt == 2000 else
+                       f"{args.n}^3 nt={args.nt} variant of: " + WORKLOAD,
+                       "grid": list(prob.shape), "nt": prob.nt, "batch_shots": C,
+                       "ckpt_k": plan.info("ckpt_k"), "tile": [plan.info("tile_x"),
+                                                              plan.info("tile_y"),
+                                                              plan.info("zchunk")],
+                       "parallelism": f"replicas{world}" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (no flush needed)"},
+            "grid_updates_per_s": value * cells * (prob.nt - 1),
+            "roofline": {"bound": "hbm", "kernel": "k_forward (3D, batched)",
+                         "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_kind": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": fwd_bytes,
+                         "launch_ms": t_launch * 1000.0},
+            "pipeline_roofline": {"bytes_per_step": pipeline_bytes,
+                                  "achieved": pipeline_bytes / (t_ms / 1000.0) / 1e9,
+                                  "frac": pipeline_bytes / (t_ms / 1000.0) / 1e9 / hbm,
+                                  "model": "44 B/shot + 20 B/batch per cell-step"},
+            "e2e": e2e, "plain": plain, "cpu_baseline": cpu,
+            "gpu_launches": launches, "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,203 @@
+/*
+ * usct_gb300.h -- C ABI of the GB300 acoustic FWI hot path (libusct_gb300.so).
+ *
+ * The library is a drop-in for the reference's acoustic wave-propagation core:
+ * the leapfrog forward solve, its exact discrete adjoint and the
+ * squared-slowness gradient, run over every transmit of a full-matrix capture.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   uap::forward_fmc          software/core/libuap.hpp:109-116
+ *   uap::misfit_and_gradient  software/core/libuap.hpp:169-224  (L2 misfit)
+ *   _uap.forward_fmc / _uap.misfit_and_gradient
+ *                             software/python/_uap.cpp:25-55   (pybind layer)
+ *   fwi.forward_fmc / misfit / misfit_and_gradient / gn_hessian_vector
+ *                             simulation/ringfwi/fwi.py:102,246,266,410
+ *                             (footprints, sponge and Born are only there)
+ *   uap_gpu.forward_fmc / misfit_and_gradient
+ *                             software/python/uap_gpu.py:166-224 (CuPy FP32)
+ *
+ * Numerics: FP32 wavefields and traces, FP64 model input, FP64 gradient
+ * accumulation and output.  Grids are row-major ([iy][ix] or [iz][iy][ix]),
+ * cells are addressed by row-major linear index, exactly as the reference's
+ * linear_indices (software/python/uap.py:19-22).  Sources and receivers are CSR
+ * lists of (cell, weight); a point element is one entry of weight 1, a
+ * finite-aperture footprint (simulation/ringfwi/geometry.py:212-278) is its
+ * cell list with weights 1/len.
+ *
+ * Every function returns 0 on success or a USCT_ERR_* code; usct_last_error()
+ * gives a one-line message for the calling thread.  Nothing here falls back to
+ * the CPU: without a CUDA device the calls fail with USCT_ERR_CUDA.
+ *
+ * Device entry points take device pointers and a CUDA stream (a cudaStream_t
+ * passed as void*; NULL = legacy default stream) and are asynchronous with
+ * respect to the host unless stated.  Scratch memory is caller-provided
+ * ("workspaces"), sized by the *_bytes queries, so callers keep control of
+ * HBM (the serving engine admits requests against these sizes).
+ */
+#ifndef USCT_GB300_H
+#define USCT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define USCT_OK 0
+#define USCT_ERR_ARG 1      /* invalid argument (shape, index out of grid, ...) */
+#define USCT_ERR_CUDA 2     /* CUDA runtime error (message has the CUDA string) */
+#define USCT_ERR_NOMEM 3    /* device allocation failed or workspace too small */
+#define USCT_ERR_STATE 4    /* call out of order (e.g. backward before forward) */
+
+/* Workspace modes for usct_batch_bytes / usct_batch_forward. */
+#define USCT_MODE_FORWARD 0   /* traces only */
+#define USCT_MODE_GRADIENT 1  /* traces + checkpoints + stash + adjoint fields */
+#define USCT_MODE_BORN 2      /* GRADIENT + the Born perturbation fields */
+
+/* usct_plan_info keys */
+#define USCT_INFO_BATCH 0        /* shot channels per batch C (power of two) */
+#define USCT_INFO_NBATCH 1       /* number of batches = ceil(n_tx / C) */
+#define USCT_INFO_CKPT_K 2       /* checkpoint interval k */
+#define USCT_INFO_NSEG 3         /* checkpoint segments ceil((nt-1)/k) */
+#define USCT_INFO_TILE_X 4       /* threads along the row (float4 each) */
+#define USCT_INFO_TILE_Y 5       /* rows per tile */
+#define USCT_INFO_ZCHUNK 6       /* planes marched per CTA */
+#define USCT_INFO_LEVEL_FLOATS 7 /* floats in one batched wavefield level */
+#define USCT_INFO_LAUNCHES 8     /* kernels launched by this plan so far */
+
+/* One-line message describing the last error on this thread ("" if none). */
+const char* usct_last_error(void);
+
+/* ABI version: major*10000 + minor*100 + patch. */
+int usct_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Plans: grid, time axis, acquisition geometry and batching, built once.   */
+/* ------------------------------------------------------------------------ */
+typedef struct usct_plan usct_plan;
+
+/*
+ * Build a plan on the current CUDA device (device memory for the per-tile
+ * source/receiver lists is allocated here and freed by usct_plan_destroy).
+ *   ndim, dims     2 -> (ny, nx), 3 -> (nz, ny, nx); every extent >= 3
+ *   h, dt, nt      grid spacing (m), time step (s), number of time levels
+ *   n_tx, tx_ptr[n_tx+1], tx_cell[], tx_w[]   source CSR, one row per transmit
+ *   n_rx, rx_ptr[n_rx+1], rx_cell[], rx_w[]   receiver CSR, one row per receiver
+ *   batch          shot channels per launch (power of two <= 64; 0 = choose)
+ *   ckpt_k         checkpoint interval in steps (0 = choose)
+ *   tile_x, tile_y, zchunk   launch shape (0 = choose); tile_x in {16,32,64,128,256}
+ * Host arrays; cells are row-major linear indices into the grid.
+ */
+int usct_plan_create(usct_plan** out, int ndim, const int* dims, double h, double dt, int nt,
+                     int n_tx, const int* tx_ptr, const int64_t* tx_cell, const double* tx_w,
+                     int n_rx, const int* rx_ptr, const int64_t* rx_cell, const double* rx_w,
+                     int batch, int ckpt_k, int tile_x, int tile_y, int zchunk);
+void usct_plan_destroy(usct_plan* plan);
+int usct_plan_info(const usct_plan* plan, int key, int64_t* value);
+
+/* Bytes of the model workspace (S, sponge, v/m, wavelet, FP64 gradient). */
+size_t usct_model_bytes(const usct_plan* plan);
+/* Bytes of one batch workspace for a USCT_MODE_*. */
+size_t usct_batch_bytes(const usct_plan* plan, int mode);
+
+/*
+ * Load the model: S = dt^2/m (libuap.hpp:73, fwi.py:52), the optional sponge
+ * mask (fwi.py:68, solver.py:22-42; NULL = none), the optional Born
+ * perturbation v (fwi.py:358, NULL = none), the wavelet; zero the gradient.
+ * m, sponge, v: device FP64, dims-shaped; wavelet: device FP64 [nt].
+ */
+int usct_model_prepare(usct_plan* plan, void* model_ws, const double* m, const double* sponge,
+                       const double* v, const double* wavelet, void* stream);
+
+/*
+ * Forward sweep of batch b (transmits b*C .. b*C+C-1) over all nt levels
+ * (fwi.py:63-79, libuap.hpp:83-104), one launch per time step for all shots
+ * of the batch.  traces (device FP32, user layout [n_tx][nt][n_rx], NULL = do
+ * not export) receives this batch's rows.  USCT_MODE_GRADIENT stores
+ * checkpoints for usct_batch_backward; USCT_MODE_BORN additionally runs the
+ * exact Born linearisation (fwi.py:350-379) in lockstep and exports the Born
+ * traces instead, keeping them as the adjoint source.
+ */
+int usct_batch_forward(usct_plan* plan, const void* model_ws, void* batch_ws, int b, int mode,
+                       float* traces, void* stream);
+
+/*
+ * L2 adjoint source of batch b from the traces of its last forward sweep:
+ * r = dsyn - dobs (libuap.hpp:125-132, fwi.py:155-157).  dobs: device FP32
+ * [n_tx][nt][n_rx]; J: device FP64 [n_tx], receives 0.5*sum r^2 per transmit
+ * of the batch (NULL = skip).
+ */
+int usct_batch_misfit(usct_plan* plan, void* batch_ws, int b, const float* dobs, double* J,
+                      void* stream);
+
+/* Use an arbitrary adjoint source for batch b (device FP32 [n_tx][nt][n_rx]),
+ * e.g. dL/d(traces) from an autograd graph. */
+int usct_batch_adjoint_source(usct_plan* plan, void* batch_ws, int b, const float* adj,
+                              void* stream);
+
+/*
+ * Backward sweep of batch b (fwi.py:306-326, libuap.hpp:196-219): the exact
+ * discrete adjoint driven by the current adjoint source, with each checkpoint
+ * segment recomputed bit-identically from its stored levels, and the imaging
+ * condition g += sum_shots lam^k * d2p^k accumulated in FP64 in model_ws.
+ */
+int usct_batch_backward(usct_plan* plan, void* model_ws, void* batch_ws, int b, void* stream);
+
+/* grad = g / m (fwi.py:331, libuap.hpp:222) into device FP64 dims-shaped
+ * grad; then zero the accumulator. */
+int usct_model_gradient(usct_plan* plan, void* model_ws, const double* m, double* grad,
+                        void* stream);
+
+/* ---- whole-acquisition device calls (loop over batches, one workspace) ---- */
+
+/* fwi.forward_fmc / uap::forward_fmc: data device FP32 [n_tx][nt][n_rx]. */
+int usct_forward_fmc_dev(usct_plan* plan, const double* m, const double* sponge,
+                         const double* wavelet, float* data, void* model_ws, void* batch_ws,
+                         void* stream);
+/* fwi.misfit_and_gradient (L2): J device FP64 [n_tx] per transmit, grad FP64. */
+int usct_misfit_and_gradient_dev(usct_plan* plan, const double* m, const double* sponge,
+                                 const double* wavelet, const float* dobs, double* J,
+                                 double* grad, void* model_ws, void* batch_ws, void* stream);
+/* fwi.gn_hessian_vector: hv device FP64 dims-shaped; born (NULL = skip) FP32
+ * [n_tx][nt][n_rx] receives J v. */
+int usct_gn_hessian_vector_dev(usct_plan* plan, const double* m, const double* sponge,
+                               const double* wavelet, const double* v, double* hv, float* born,
+                               void* model_ws, void* batch_ws, void* stream);
+
+/* ---- the plain one-shot-per-launch GPU form (the comparison baseline) ---- */
+/*
+ * A restatement of the reference's CuPy backend (software/python/uap_gpu.py:
+ * 100-140): one thread per cell, separate launches per time step for the
+ * stencil, source injection, receiver gather, history copy, adjoint step,
+ * adjoint injection and imaging; the full FP32 history is kept in HBM.
+ * Point elements only (as the reference's GPU backend).  It exists to measure
+ * the batched engine against; it shares no kernel with it.
+ */
+size_t usct_plain_bytes(const usct_plan* plan, int gradient);
+int usct_plain_forward_fmc_dev(usct_plan* plan, const double* m, const double* wavelet,
+                               float* data, void* ws, void* stream);
+int usct_plain_misfit_and_gradient_dev(usct_plan* plan, const double* m, const double* wavelet,
+                                       const float* dobs, double* J, double* grad, void* ws,
+                                       void* stream);
+
+/* ---- host-pointer calls with the reference core's own signatures ---- */
+/*
+ * Same arguments and layouts as uap::forward_fmc (libuap.hpp:109) and
+ * uap::misfit_and_gradient (libuap.hpp:169, misfit_type 0 only): host FP64
+ * arrays in, host FP64 out; point elements tx_lin[n_tx], rec_lin[n_rec].
+ * These allocate device memory for the duration of the call, copy in, run on
+ * the legacy default stream and copy out (synchronous).
+ */
+int usct_forward_fmc(const double* m, const int* dims, int ndim, double h, double dt, int nt,
+                     const int* tx_lin, int n_tx, const int* rec_lin, int n_rec,
+                     const double* wavelet, double* data);
+int usct_misfit_and_gradient(const double* m, const int* dims, int ndim, double h, double dt,
+                             int nt, const int* tx_lin, int n_tx, const int* rec_lin, int n_rec,
+                             const double* wavelet, const double* dobs, double* grad, double* J);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* USCT_GB300_H */

@@ -1,0 +1,326 @@
+"""GB300 backend with the reference's backend protocol.
+
+Use it wherever the reference accepts a ``backend=`` module::
+
+    from ringfwi import fwi
+    import openusct_gb300.backend as gb300
+    m, hist = fwi.invert(m0, geom, wavelet, dt, h, nt, dobs, backend=gb300)
+    plugins.run("fwi", dataset, backend=gb300)
+
+Signatures follow ``simulation/ringfwi/fwi.py`` (forward_fmc :102, misfit :246,
+misfit_and_gradient :266, gn_hessian_vector :410), which is the superset of the
+reference's C++ (software/python/uap.py:34-67) and CuPy
+(software/python/uap_gpu.py:166-233) backends; inputs are NumPy arrays (or CUDA
+tensors), outputs are FP64 NumPy arrays like the reference's.  Error behaviour
+follows the reference GPU backend: a non-L2 misfit raises NotImplementedError
+(uap_gpu.py:191-192), an unknown one ValueError (fwi.py:243).
+
+Everything runs on the CUDA kernels of ``libusct_gb300.so``; a missing library
+or device raises instead of falling back to the CPU.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from collections import OrderedDict
+
+import numpy as np
+import torch
+
+from . import _lib
+from .geometry import CSR, element_csr
+
+_KNOWN_MISFITS = ("l2", "gcn", "envelope", "egcn", "gsot", "traveltime")
+
+
+def _ptr(t):
+    return ctypes.c_void_p(0 if t is None else t.data_ptr())
+
+
+def _stream(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("openusct_gb300 needs a CUDA device (there is no CPU fallback)")
+
+
+def _to_dev(x, dtype, device):
+    if x is None:
+        return None
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=dtype).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64 if dtype == torch.float64
+                                                 else np.float32)).to(device)
+
+
+class Plan:
+    """A ``usct_plan``: grid, time axis, elements and batching on one device."""
+
+    def __init__(self, shape, h, dt, nt, tx: CSR, rx: CSR, batch=0, ckpt_k=0, tile_x=0,
+                 tile_y=0, zchunk=0):
+        _require_cuda()
+        lib = _lib.load()
+        self.shape = tuple(int(s) for s in shape)
+        self.h, self.dt, self.nt = float(h), float(dt), int(nt)
+        self.tx, self.rx = tx, rx
+        self.n_tx, self.n_rx = tx.rows, rx.rows
+        dims = (ctypes.c_int * len(self.shape))(*self.shape)
+        self._keep = (tx, rx)
+        ptr = ctypes.c_void_p()
+        _lib.check(lib.usct_plan_create(
+            ctypes.byref(ptr), len(self.shape), dims, self.h, self.dt, self.nt,
+            tx.rows, tx.ptr.ctypes.data_as(_lib._ip), tx.cell.ctypes.data_as(_lib._lp),
+            tx.w.ctypes.data_as(_lib._dp), rx.rows, rx.ptr.ctypes.data_as(_lib._ip),
+            rx.cell.ctypes.data_as(_lib._lp), rx.w.ctypes.data_as(_lib._dp), int(batch),
+            int(ckpt_k), int(tile_x), int(tile_y), int(zchunk)))
+        self._p = ptr
+        self._lib = lib
+
+    @property
+    def handle(self):
+        return self._p
+
+    def info(self, key):
+        v = ctypes.c_int64()
+        _lib.check(self._lib.usct_plan_info(self._p, _lib.INFO[key], ctypes.byref(v)))
+        return int(v.value)
+
+    @property
+    def batch(self):
+        return self.info("batch")
+
+    @property
+    def nbatch(self):
+        return self.info("nbatch")
+
+    def model_bytes(self):
+        return int(self._lib.usct_model_bytes(self._p))
+
+    def batch_bytes(self, mode):
+        return int(self._lib.usct_batch_bytes(self._p, int(mode)))
+
+    def plain_bytes(self, gradient):
+        return int(self._lib.usct_plain_bytes(self._p, int(bool(gradient))))
+
+    def close(self):
+        if getattr(self, "_p", None) is not None and self._p.value:
+            self._lib.usct_plan_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_bytes_estimate(shape, nt, n_rx, nslot, C, ckpt_k, mode):
+    """Bytes of one batch workspace (mirrors usct_batch_bytes)."""
+    al = lambda x: (x + 255) // 256 * 256  # noqa: E731
+    nx = shape[-1]
+    nxs = (nx + 3) // 4 * 4
+    rows = int(np.prod(shape[:-1]))
+    lv = al(rows * nxs * C * 4)
+    k = ckpt_k if ckpt_k else max(2, int(round((2.0 * (nt - 1)) ** 0.5)))
+    k = min(k, max(2, nt - 1))
+    nseg = (nt - 1 + k - 1) // k
+    b = 2 * lv + al(nt * nslot * C * 4) + al(nt * n_rx * C * 4) + al(64 * C * 8)
+    if mode >= _lib.MODE_GRADIENT:
+        b += (2 + 2 * nseg + k) * lv
+    if mode == _lib.MODE_BORN:
+        b += 2 * lv
+    return b
+
+
+def choose_batch(shape, nt, n_tx, n_rx, nslot, ckpt_k, mode, budget):
+    """Widest power-of-two shot batch (<= 64) whose workspace fits ``budget``."""
+    C = 1
+    while C < n_tx and C < 64:
+        C *= 2
+    while C > 1 and batch_bytes_estimate(shape, nt, n_rx, nslot, C, ckpt_k, mode) > budget:
+        C //= 2
+    return C
+
+
+_PLANS: "OrderedDict[tuple, Plan]" = OrderedDict()
+_MAX_PLANS = 8
+
+
+def get_plan(shape, h, dt, nt, tx, rx, batch=0, ckpt_k=0, tile_x=0, tile_y=0, zchunk=0):
+    key = (tuple(shape), float(h), float(dt), int(nt), tx.key(), rx.key(), int(batch),
+           int(ckpt_k), int(tile_x), int(tile_y), int(zchunk), torch.cuda.current_device())
+    p = _PLANS.get(key)
+    if p is None:
+        p = Plan(shape, h, dt, nt, tx, rx, batch, ckpt_k, tile_x, tile_y, zchunk)
+        _PLANS[key] = p
+        while len(_PLANS) > _MAX_PLANS:
+            _PLANS.popitem(last=False)[1].close()
+    else:
+        _PLANS.move_to_end(key)
+    return p
+
+
+def _setup(m, geom, h, dt, nt, src_list, footprints, mode, batch, ckpt_k, tile):
+    _require_cuda()
+    shape = tuple(np.shape(m))
+    if len(shape) not in (2, 3):
+        raise ValueError(f"model must be 2D or 3D, got shape {shape}")
+    tx, rx = element_csr(geom, shape, src_list, footprints)
+    if not batch:
+        free, _total = torch.cuda.mem_get_info()
+        budget = int(0.7 * free)
+        batch = choose_batch(shape, nt, rx.rows, len(rx.cell), ckpt_k or 0, mode, budget)
+    tile = tile or (0, 0, 0)
+    return get_plan(shape, h, dt, nt, tx, rx, batch, ckpt_k or 0, *tile)
+
+
+def _workspace(nbytes, device):
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+
+
+def _out(x, like):
+    """Host FP64 NumPy output unless the caller passed CUDA tensors."""
+    if isinstance(like, torch.Tensor) and like.is_cuda:
+        return x
+    return x.detach().cpu().numpy().astype(np.float64)
+
+
+def _check_misfit(misfit_type, time_weights):
+    if misfit_type not in _KNOWN_MISFITS:
+        raise ValueError(f"unknown misfit_type {misfit_type!r}")
+    if misfit_type != "l2":
+        raise NotImplementedError("the GB300 backend implements the L2 misfit only")
+    if time_weights is not None:
+        raise NotImplementedError("time_weights are not supported by the GB300 backend")
+
+
+# ---------------------------------------------------------------------------
+# public API (signature-compatible with ringfwi.fwi)
+# ---------------------------------------------------------------------------
+def forward_fmc(m, geom, wavelet, dt, h, nt, sponge=None, src_list=None, footprints=None, *,
+                batch=None, tile=None):
+    """Full-matrix capture: data[i, n, j] = receiver j at level n for transmit i."""
+    plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_FORWARD, batch, None, tile)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    md = _to_dev(m, torch.float64, dev)
+    wd = _to_dev(wavelet, torch.float64, dev)
+    sd = _to_dev(sponge, torch.float64, dev)
+    data = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev)
+    mws = _workspace(plan.model_bytes(), dev)
+    bws = _workspace(plan.batch_bytes(_lib.MODE_FORWARD), dev)
+    _lib.check(plan._lib.usct_forward_fmc_dev(plan.handle, _ptr(md), _ptr(sd), _ptr(wd),
+                                              _ptr(data), _ptr(mws), _ptr(bws), _stream()))
+    return _out(data, m)
+
+
+def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None,
+                        misfit_type="l2", footprints=None, time_weights=None, *, batch=None,
+                        ckpt_k=None, tile=None, return_per_shot=False):
+    """L2 waveform misfit and its exact discrete-adjoint gradient in m (FP64)."""
+    _check_misfit(misfit_type, time_weights)
+    plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_GRADIENT, batch, ckpt_k,
+                  tile)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    md = _to_dev(m, torch.float64, dev)
+    wd = _to_dev(wavelet, torch.float64, dev)
+    sd = _to_dev(sponge, torch.float64, dev)
+    od = _to_dev(dobs, torch.float32, dev)
+    if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
+        raise ValueError(f"dobs has shape {tuple(od.shape)}, expected "
+                         f"{(plan.n_tx, plan.nt, plan.n_rx)}")
+    J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
+    g = torch.empty(plan.shape, dtype=torch.float64, device=dev)
+    mws = _workspace(plan.model_bytes(), dev)
+    bws = _workspace(plan.batch_bytes(_lib.MODE_GRADIENT), dev)
+    _lib.check(plan._lib.usct_misfit_and_gradient_dev(
+        plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(od), _ptr(J), _ptr(g), _ptr(mws),
+        _ptr(bws), _stream()))
+    Jh = J.cpu().numpy()
+    Jv = float(np.sum(Jh))
+    if return_per_shot:
+        return Jv, _out(g, m), Jh
+    return Jv, _out(g, m)
+
+
+def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, misfit_type="l2",
+           footprints=None, time_weights=None, *, batch=None, tile=None):
+    """L2 waveform misfit only (one forward sweep per batch)."""
+    _check_misfit(misfit_type, time_weights)
+    plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_FORWARD, batch, None, tile)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    md = _to_dev(m, torch.float64, dev)
+    wd = _to_dev(wavelet, torch.float64, dev)
+    sd = _to_dev(sponge, torch.float64, dev)
+    od = _to_dev(dobs, torch.float32, dev)
+    if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
+        raise ValueError("dobs shape does not match the acquisition")
+    J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
+    mws = _workspace(plan.model_bytes(), dev)
+    bws = _workspace(plan.batch_bytes(_lib.MODE_FORWARD), dev)
+    lib, s = plan._lib, _stream()
+    _lib.check(lib.usct_model_prepare(plan.handle, _ptr(mws), _ptr(md), _ptr(sd), None, _ptr(wd), s))
+    for b in range(plan.nbatch):
+        _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
+                                          _lib.MODE_FORWARD, None, s))
+        _lib.check(lib.usct_batch_misfit(plan.handle, _ptr(bws), b, _ptr(od), _ptr(J), s))
+    return float(np.sum(J.cpu().numpy()))
+
+
+def gn_hessian_vector(m, geom, wavelet, dt, h, nt, v, sponge=None, src_list=None,
+                      footprints=None, wavefields=None, *, batch=None, ckpt_k=None, tile=None,
+                      return_born=False):
+    """Gauss-Newton product sum_s J_s^T J_s v (exact Born + exact adjoint).
+
+    ``wavefields`` is accepted for signature compatibility and ignored: the
+    background is recomputed from checkpoints on the device.
+    """
+    del wavefields
+    plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_BORN, batch, ckpt_k, tile)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    md = _to_dev(m, torch.float64, dev)
+    wd = _to_dev(wavelet, torch.float64, dev)
+    sd = _to_dev(sponge, torch.float64, dev)
+    vd = _to_dev(v, torch.float64, dev)
+    hv = torch.empty(plan.shape, dtype=torch.float64, device=dev)
+    born = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev) \
+        if return_born else None
+    mws = _workspace(plan.model_bytes(), dev)
+    bws = _workspace(plan.batch_bytes(_lib.MODE_BORN), dev)
+    _lib.check(plan._lib.usct_gn_hessian_vector_dev(
+        plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(vd), _ptr(hv), _ptr(born), _ptr(mws),
+        _ptr(bws), _stream()))
+    if return_born:
+        return _out(hv, m), _out(born, m)
+    return _out(hv, m)
+
+
+# ---------------------------------------------------------------------------
+# the plain one-shot-per-launch GPU form (comparison baseline)
+# ---------------------------------------------------------------------------
+def plain_forward_fmc(m, geom, wavelet, dt, h, nt, src_list=None):
+    plan = _setup(m, geom, h, dt, nt, src_list, None, _lib.MODE_FORWARD, 1, None, None)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    md = _to_dev(m, torch.float64, dev)
+    wd = _to_dev(wavelet, torch.float64, dev)
+    data = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev)
+    ws = _workspace(plan.plain_bytes(False), dev)
+    _lib.check(plan._lib.usct_plain_forward_fmc_dev(plan.handle, _ptr(md), _ptr(wd), _ptr(data),
+                                                    _ptr(ws), _stream()))
+    return _out(data, m)
+
+
+def plain_misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, src_list=None):
+    plan = _setup(m, geom, h, dt, nt, src_list, None, _lib.MODE_FORWARD, 1, None, None)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    md = _to_dev(m, torch.float64, dev)
+    wd = _to_dev(wavelet, torch.float64, dev)
+    od = _to_dev(dobs, torch.float32, dev)
+    J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
+    g = torch.empty(plan.shape, dtype=torch.float64, device=dev)
+    ws = _workspace(plan.plain_bytes(True), dev)
+    _lib.check(plan._lib.usct_plain_misfit_and_gradient_dev(
+        plan.handle, _ptr(md), _ptr(wd), _ptr(od), _ptr(J), _ptr(g), _ptr(ws), _stream()))
+    return float(np.sum(J.cpu().numpy())), _out(g, m)

@@ -1,0 +1,58 @@
+"""Build recipe for the CUDA library ``openusct_gb300/libusct_gb300.so``.
+
+One translation unit, one ``-gencode`` (sm_103a), built in-tree with nvcc.
+``-fmad=false`` keeps every multiply-add unfused unless the kernels ask for
+``__fmaf_rn`` explicitly, which fixes the rounding of the stencil so the CPU
+restatement can reproduce it bit for bit.
+"""
+
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+LIB = os.path.join(PKG, "libusct_gb300.so")
+SOURCES = ["usct_engine.cu"]
+DEPS = ["usct_engine.cu", "usct_kernels.cuh", "usct_plain.cuh"]
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libusct_gb300.so")
+
+
+def command(out: str = LIB, verbose_ptxas: bool = False) -> list[str]:
+    cmd = [nvcc(), ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17",
+           "-Xcompiler", "-fPIC", "-shared", "-I", os.path.join(REPO, "include"),
+           "-o", out] + [os.path.join(CSRC, s) for s in SOURCES]
+    if verbose_ptxas:
+        cmd.insert(1, "-Xptxas=-v")
+    return cmd
+
+
+def up_to_date(out: str = LIB) -> bool:
+    if not os.path.exists(out):
+        return False
+    t = os.path.getmtime(out)
+    deps = [os.path.join(CSRC, d) for d in DEPS] + [os.path.join(REPO, "include", "usct_gb300.h")]
+    return all(os.path.getmtime(d) <= t for d in deps)
+
+
+def build(force: bool = False, verbose_ptxas: bool = False) -> str:
+    """Compile the library if a source is newer than it; return its path."""
+    if force or not up_to_date():
+        tmp = LIB + ".tmp"
+        subprocess.run(command(tmp, verbose_ptxas), check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force=True, verbose_ptxas=True)

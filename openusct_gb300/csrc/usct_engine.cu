@@ -1,0 +1,862 @@
+// usct_engine.cu -- host side of the batched engine behind the C ABI in
+// include/usct_gb300.h: plans, workspace carving, the checkpointed time loops
+// and the small gather/prepare kernels.
+//
+// Time loops (one launch per time step for all C shots of a batch):
+//   forward   n = 1..nt-1: p^n from (p^{n-1}, p^{n-2}) in two ping-pong
+//             buffers; receivers sampled into slot rows; the pair
+//             (p^{a-1}, p^a) copied out at every segment start a = j*k; the
+//             last segment's d2p written straight into the stash.
+//   backward  segments j = nseg-1..0: recompute levels a+1..b from the stored
+//             pair with the same kernel (bit-identical), stashing d2p; then
+//             adjoint steps k = b..a+1 consuming the stash (fwi.py:310-330).
+// Memory per batch (levels of nz*ny*nxs*C floats): 2 state + 2*nseg
+// checkpoints + k stash + 2 adjoint (+2 Born), see usct_batch_bytes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "usct_gb300.h"
+#include "usct_kernels.cuh"
+
+using namespace usct;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_err;
+
+static int set_err(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CUDA_TRY(x)                                                                     \
+    do {                                                                                \
+        cudaError_t e_ = (x);                                                           \
+        if (e_ != cudaSuccess)                                                          \
+            return set_err(e_ == cudaErrorMemoryAllocation ? USCT_ERR_NOMEM : USCT_ERR_CUDA, \
+                           "%s: %s", #x, cudaGetErrorString(e_));                       \
+    } while (0)
+
+#define TRY(x)                   \
+    do {                         \
+        int r_ = (x);            \
+        if (r_ != USCT_OK) return r_; \
+    } while (0)
+
+extern "C" const char* usct_last_error(void) { return g_err.c_str(); }
+extern "C" int usct_version(void) { return 10000; }
+
+// ---------------------------------------------------------------------------
+// plan
+// ---------------------------------------------------------------------------
+struct usct_plan {
+    int device = 0;
+    int ndim = 0;
+    int dims[3] = {0, 0, 0};
+    double h = 0, dt = 0;
+    int nt = 0, n_tx = 0, n_rx = 0;
+    Geo geo{};
+    int txv = 0, ty = 0, nzc = 0, ntx_t = 0, nty_t = 0, ntiles = 0;
+    int C = 0, logC = 0, nbatch = 0, k = 0, nseg = 0;
+    size_t N = 0, cells_p = 0, LV = 0;
+    int nslot = 0;
+    int* d_sptr = nullptr;
+    SrcEnt* d_sent = nullptr;
+    int* d_rptr = nullptr;
+    RxEnt* d_rent = nullptr;
+    int* d_rxptr = nullptr;
+    // plain one-shot form (point elements): cells and weights per transmit/receiver
+    std::vector<int> h_tx_ptr, h_rx_ptr;
+    std::vector<int64_t> h_tx_cell, h_rx_cell;
+    std::vector<double> h_tx_w, h_rx_w;
+    int64_t* d_tx_cell = nullptr;
+    float* d_tx_w = nullptr;
+    int64_t* d_rx_cell = nullptr;
+    bool has_sp = false, has_vm = false;
+    long long launches = 0;
+};
+
+static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+static int ilog2(int c) { int l = 0; while ((1 << l) < c) ++l; return l; }
+static bool pow2(int c) { return c > 0 && (c & (c - 1)) == 0; }
+
+static bool tile_supported(bool is3d, int txv, int ty) {
+    if (is3d) return (txv == 32 && (ty == 4 || ty == 8)) || (txv == 64 && (ty == 2 || ty == 4));
+    return ty == 1 && (txv == 64 || txv == 128);
+}
+
+static void free_plan_dev(usct_plan* p) {
+    cudaFree(p->d_sptr); cudaFree(p->d_sent); cudaFree(p->d_rptr); cudaFree(p->d_rent);
+    cudaFree(p->d_rxptr); cudaFree(p->d_tx_cell); cudaFree(p->d_tx_w); cudaFree(p->d_rx_cell);
+    p->d_sptr = nullptr; p->d_sent = nullptr; p->d_rptr = nullptr; p->d_rent = nullptr;
+    p->d_rxptr = nullptr; p->d_tx_cell = nullptr; p->d_tx_w = nullptr; p->d_rx_cell = nullptr;
+}
+
+template <class T>
+static int upload(T** dst, const std::vector<T>& v) {
+    const size_t n = std::max<size_t>(v.size(), 1);
+    CUDA_TRY(cudaMalloc(dst, n * sizeof(T)));
+    if (!v.empty()) CUDA_TRY(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return USCT_OK;
+}
+
+static int check_csr(const char* what, int n, const int* ptr, const int64_t* cell, const double* w,
+                     int64_t ncell) {
+    if (!ptr) return set_err(USCT_ERR_ARG, "%s: null pointer array", what);
+    if (ptr[0] != 0) return set_err(USCT_ERR_ARG, "%s: ptr[0] must be 0", what);
+    for (int i = 0; i < n; ++i)
+        if (ptr[i + 1] < ptr[i]) return set_err(USCT_ERR_ARG, "%s: ptr not monotone at %d", what, i);
+    const int ne = ptr[n];
+    if (ne > 0 && (!cell || !w)) return set_err(USCT_ERR_ARG, "%s: null cell/weight array", what);
+    for (int e = 0; e < ne; ++e) {
+        if (cell[e] < 0 || cell[e] >= ncell)
+            return set_err(USCT_ERR_ARG, "%s: cell %lld of entry %d outside the grid (%lld cells)",
+                           what, (long long)cell[e], e, (long long)ncell);
+        if (!std::isfinite(w[e])) return set_err(USCT_ERR_ARG, "%s: non-finite weight at %d", what, e);
+    }
+    return USCT_OK;
+}
+
+// cell -> (z, y, x) in the engine's axis convention (2D: z = row, y = 0)
+static void unravel(const usct_plan* p, int64_t cell, int& z, int& y, int& x) {
+    const int nx = p->geo.nx, ny = p->geo.ny;
+    x = (int)(cell % nx);
+    const int64_t r = cell / nx;
+    y = (int)(r % ny);
+    z = (int)(r / ny);
+}
+
+extern "C" int usct_plan_create(usct_plan** out, int ndim, const int* dims, double h, double dt,
+                                int nt, int n_tx, const int* tx_ptr, const int64_t* tx_cell,
+                                const double* tx_w, int n_rx, const int* rx_ptr,
+                                const int64_t* rx_cell, const double* rx_w, int batch, int ckpt_k,
+                                int tile_x, int tile_y, int zchunk) {
+    if (!out) return set_err(USCT_ERR_ARG, "out is null");
+    *out = nullptr;
+    if (ndim != 2 && ndim != 3) return set_err(USCT_ERR_ARG, "ndim must be 2 or 3 (got %d)", ndim);
+    if (!dims) return set_err(USCT_ERR_ARG, "dims is null");
+    for (int d = 0; d < ndim; ++d)
+        if (dims[d] < 3) return set_err(USCT_ERR_ARG, "dims[%d] = %d < 3", d, dims[d]);
+    if (nt < 2) return set_err(USCT_ERR_ARG, "nt must be >= 2 (got %d)", nt);
+    if (!(h > 0) || !(dt > 0)) return set_err(USCT_ERR_ARG, "h and dt must be positive");
+    if (n_tx < 1 || n_rx < 1) return set_err(USCT_ERR_ARG, "need at least one transmit and one receiver");
+    if (batch != 0 && (!pow2(batch) || batch > 64))
+        return set_err(USCT_ERR_ARG, "batch must be a power of two <= 64 (got %d)", batch);
+    if (ckpt_k != 0 && ckpt_k < 2) return set_err(USCT_ERR_ARG, "ckpt_k must be >= 2 (got %d)", ckpt_k);
+
+    usct_plan* p = new usct_plan();
+    cudaGetDevice(&p->device);
+    p->ndim = ndim;
+    for (int d = 0; d < ndim; ++d) p->dims[d] = dims[d];
+    p->h = h; p->dt = dt; p->nt = nt; p->n_tx = n_tx; p->n_rx = n_rx;
+    Geo& g = p->geo;
+    if (ndim == 3) { g.nz = dims[0]; g.ny = dims[1]; g.nx = dims[2]; }
+    else { g.nz = dims[0]; g.ny = 1; g.nx = dims[1]; }
+    p->N = (size_t)g.nz * g.ny * g.nx;
+    int ret = check_csr("sources", n_tx, tx_ptr, tx_cell, tx_w, (int64_t)p->N);
+    if (ret == USCT_OK) ret = check_csr("receivers", n_rx, rx_ptr, rx_cell, rx_w, (int64_t)p->N);
+    if (ret != USCT_OK) { delete p; return ret; }
+
+    int C = batch;
+    if (C == 0) { C = 1; while (C < n_tx && C < 32) C <<= 1; }
+    p->C = C; p->logC = ilog2(C);
+    p->nbatch = (n_tx + C - 1) / C;
+    g.C = C; g.logC = p->logC;
+    g.nxs = (g.nx + 3) & ~3;
+    g.RP = g.nxs * C;
+    g.PP = (long long)g.RP * g.ny;
+    g.CPP = (long long)g.nxs * g.ny;
+    g.inv_h2 = (float)(1.0 / (h * h));
+    p->cells_p = (size_t)g.CPP * g.nz;
+    p->LV = (size_t)g.PP * g.nz;
+
+    const bool is3d = ndim == 3;
+    int txv = tile_x, ty = tile_y;
+    if (txv == 0) txv = is3d ? (C >= 16 ? 64 : 32) : 128;
+    if (ty == 0 || !is3d) ty = is3d ? (txv == 64 ? 4 : 8) : 1;
+    if (!tile_supported(is3d, txv, ty)) {
+        delete p;
+        return set_err(USCT_ERR_ARG, "unsupported tile %dx%d for %dD", txv, ty, ndim);
+    }
+    if (4 * txv < C) { delete p; return set_err(USCT_ERR_ARG, "tile row narrower than the batch"); }
+    p->txv = txv; p->ty = ty;
+    p->ntx_t = (g.RP + 4 * txv - 1) / (4 * txv);
+    p->nty_t = (g.ny + ty - 1) / ty;
+    p->ntiles = p->ntx_t * p->nty_t;
+    g.ntiles_x = p->ntx_t;
+    int zc = zchunk;
+    if (zc <= 0) {
+        const long long target = 152LL * 16;   // CTAs for a few full waves
+        long long nzc = (target + p->ntiles - 1) / p->ntiles;
+        nzc = std::max<long long>(1, std::min<long long>(nzc, g.nz / 8 > 0 ? g.nz / 8 : 1));
+        zc = (int)((g.nz + nzc - 1) / nzc);
+    }
+    zc = std::max(1, std::min(zc, g.nz));
+    g.zc = zc;
+    p->nzc = (g.nz + zc - 1) / zc;
+    if (p->nty_t > 65535 || p->nzc > 65535) { delete p; return set_err(USCT_ERR_ARG, "grid too large"); }
+
+    int k = ckpt_k;
+    if (k == 0) {
+        k = (int)std::lround(std::sqrt(2.0 * (nt - 1)));
+        k = std::max(2, k);
+    }
+    k = std::min(k, std::max(2, nt - 1));
+    p->k = k;
+    p->nseg = (nt - 1 + k - 1) / k;
+
+    // plain-form copies
+    p->h_tx_ptr.assign(tx_ptr, tx_ptr + n_tx + 1);
+    p->h_rx_ptr.assign(rx_ptr, rx_ptr + n_rx + 1);
+    p->h_tx_cell.assign(tx_cell, tx_cell + tx_ptr[n_tx]);
+    p->h_rx_cell.assign(rx_cell, rx_cell + rx_ptr[n_rx]);
+    p->h_tx_w.assign(tx_w, tx_w + tx_ptr[n_tx]);
+    p->h_rx_w.assign(rx_w, rx_w + rx_ptr[n_rx]);
+
+    // per-tile source entries, per batch
+    const int TXF = 4 * txv, cpt = TXF / C;   // cells per tile row
+    std::vector<int> sptr((size_t)p->nbatch * (p->ntiles + 1), 0);
+    std::vector<SrcEnt> sent;
+    for (int b = 0; b < p->nbatch; ++b) {
+        std::vector<std::pair<int, SrcEnt>> tmp;   // (tile, entry)
+        for (int c = 0; c < C; ++c) {
+            const int t = b * C + c;
+            if (t >= n_tx) break;
+            for (int e = tx_ptr[t]; e < tx_ptr[t + 1]; ++e) {
+                int z, y, x;
+                unravel(p, tx_cell[e], z, y, x);
+                const int xt = x / cpt, yt = y / ty;
+                SrcEnt se{z, y - yt * ty, (x - xt * cpt) * C + c, (float)tx_w[e]};
+                tmp.push_back({xt + p->ntx_t * yt, se});
+            }
+        }
+        std::stable_sort(tmp.begin(), tmp.end(), [](const auto& a, const auto& b2) {
+            return a.first != b2.first ? a.first < b2.first : a.second.z < b2.second.z;
+        });
+        int* bp = &sptr[(size_t)b * (p->ntiles + 1)];
+        const int base = (int)sent.size();
+        size_t q = 0;
+        for (int tl = 0; tl < p->ntiles; ++tl) {
+            bp[tl] = base + (int)q;
+            while (q < tmp.size() && tmp[q].first == tl) { sent.push_back(tmp[q].second); ++q; }
+        }
+        bp[p->ntiles] = base + (int)q;
+    }
+    // per-tile receiver entries (shared by all batches), ordered (z, ly, lcell, j)
+    std::vector<std::pair<int, RxEnt>> rtmp;
+    for (int j = 0; j < n_rx; ++j)
+        for (int e = rx_ptr[j]; e < rx_ptr[j + 1]; ++e) {
+            int z, y, x;
+            unravel(p, rx_cell[e], z, y, x);
+            const int xt = x / cpt, yt = y / ty;
+            RxEnt re{z, y - yt * ty, x - xt * cpt, e, j, (float)rx_w[e], 0, 0};
+            rtmp.push_back({xt + p->ntx_t * yt, re});
+        }
+    std::stable_sort(rtmp.begin(), rtmp.end(), [](const auto& a, const auto& b2) {
+        if (a.first != b2.first) return a.first < b2.first;
+        if (a.second.z != b2.second.z) return a.second.z < b2.second.z;
+        if (a.second.ly != b2.second.ly) return a.second.ly < b2.second.ly;
+        return a.second.lcell < b2.second.lcell;
+    });
+    std::vector<int> rptr(p->ntiles + 1, 0);
+    std::vector<RxEnt> rent;
+    {
+        size_t q = 0;
+        for (int tl = 0; tl < p->ntiles; ++tl) {
+            rptr[tl] = (int)q;
+            while (q < rtmp.size() && rtmp[q].first == tl) { rent.push_back(rtmp[q].second); ++q; }
+        }
+        rptr[p->ntiles] = (int)q;
+    }
+    p->nslot = rx_ptr[n_rx];
+    std::vector<int> rxptr(rx_ptr, rx_ptr + n_rx + 1);
+    std::vector<float> txwf(p->h_tx_w.begin(), p->h_tx_w.end());
+
+    if ((ret = upload(&p->d_sptr, sptr)) != USCT_OK || (ret = upload(&p->d_sent, sent)) != USCT_OK ||
+        (ret = upload(&p->d_rptr, rptr)) != USCT_OK || (ret = upload(&p->d_rent, rent)) != USCT_OK ||
+        (ret = upload(&p->d_rxptr, rxptr)) != USCT_OK ||
+        (ret = upload(&p->d_tx_cell, p->h_tx_cell)) != USCT_OK ||
+        (ret = upload(&p->d_tx_w, txwf)) != USCT_OK ||
+        (ret = upload(&p->d_rx_cell, p->h_rx_cell)) != USCT_OK) {
+        free_plan_dev(p);
+        delete p;
+        return ret;
+    }
+    *out = p;
+    return USCT_OK;
+}
+
+extern "C" void usct_plan_destroy(usct_plan* p) {
+    if (!p) return;
+    free_plan_dev(p);
+    delete p;
+}
+
+extern "C" int usct_plan_info(const usct_plan* p, int key, int64_t* value) {
+    if (!p || !value) return set_err(USCT_ERR_ARG, "null argument");
+    switch (key) {
+        case USCT_INFO_BATCH: *value = p->C; break;
+        case USCT_INFO_NBATCH: *value = p->nbatch; break;
+        case USCT_INFO_CKPT_K: *value = p->k; break;
+        case USCT_INFO_NSEG: *value = p->nseg; break;
+        case USCT_INFO_TILE_X: *value = p->txv; break;
+        case USCT_INFO_TILE_Y: *value = p->ty; break;
+        case USCT_INFO_ZCHUNK: *value = p->geo.zc; break;
+        case USCT_INFO_LEVEL_FLOATS: *value = (int64_t)p->LV; break;
+        case USCT_INFO_LAUNCHES: *value = p->launches; break;
+        default: return set_err(USCT_ERR_ARG, "unknown info key %d", key);
+    }
+    return USCT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// workspaces
+// ---------------------------------------------------------------------------
+struct ModelWS {
+    float* S; float* sp; float* vm; float* wav; double* g;
+};
+static const int JBLK = 64;   // gather blocks (per-block FP64 misfit partials)
+
+static ModelWS carve_model(const usct_plan* p, void* base) {
+    char* c = (char*)base;
+    ModelWS m;
+    const size_t cf = al256(p->cells_p * sizeof(float));
+    m.S = (float*)c; c += cf;
+    m.sp = (float*)c; c += cf;
+    m.vm = (float*)c; c += cf;
+    m.wav = (float*)c; c += al256((size_t)p->nt * sizeof(float));
+    m.g = (double*)c;
+    return m;
+}
+
+extern "C" size_t usct_model_bytes(const usct_plan* p) {
+    if (!p) return 0;
+    return 3 * al256(p->cells_p * sizeof(float)) + al256((size_t)p->nt * sizeof(float)) +
+           al256(p->cells_p * sizeof(double));
+}
+
+struct BatchWS {
+    float* P[2]; float* rs; float* res; double* jpart; float* ck; float* stash; float* L[2]; float* D[2];
+};
+
+static BatchWS carve_batch(const usct_plan* p, void* base, int mode) {
+    char* c = (char*)base;
+    BatchWS w{};
+    const size_t lv = al256(p->LV * sizeof(float));
+    w.P[0] = (float*)c; c += lv;
+    w.P[1] = (float*)c; c += lv;
+    w.rs = (float*)c; c += al256((size_t)p->nt * p->nslot * p->C * sizeof(float));
+    w.res = (float*)c; c += al256((size_t)p->nt * p->n_rx * p->C * sizeof(float));
+    w.jpart = (double*)c; c += al256((size_t)JBLK * p->C * sizeof(double));
+    if (mode >= USCT_MODE_GRADIENT) {
+        w.L[0] = (float*)c; c += lv;
+        w.L[1] = (float*)c; c += lv;
+        w.ck = (float*)c; c += (size_t)p->nseg * 2 * lv;
+        w.stash = (float*)c; c += (size_t)p->k * lv;
+    }
+    if (mode == USCT_MODE_BORN) {
+        w.D[0] = (float*)c; c += lv;
+        w.D[1] = (float*)c; c += lv;
+    }
+    return w;
+}
+
+extern "C" size_t usct_batch_bytes(const usct_plan* p, int mode) {
+    if (!p || mode < 0 || mode > 2) return 0;
+    const size_t lv = al256(p->LV * sizeof(float));
+    size_t b = 2 * lv + al256((size_t)p->nt * p->nslot * p->C * sizeof(float)) +
+               al256((size_t)p->nt * p->n_rx * p->C * sizeof(float)) +
+               al256((size_t)JBLK * p->C * sizeof(double));
+    if (mode >= USCT_MODE_GRADIENT) b += (2 + 2 * (size_t)p->nseg + (size_t)p->k) * lv;
+    if (mode == USCT_MODE_BORN) b += 2 * lv;
+    return b;
+}
+
+// ---------------------------------------------------------------------------
+// small kernels
+// ---------------------------------------------------------------------------
+__global__ void k_prepare(const double* __restrict__ m, const double* __restrict__ sp,
+                          const double* __restrict__ v, float* S, float* spo, float* vm, double dt2,
+                          int nx, int nxs, long long ncp) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ncp;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % nxs);
+        const long long r = i / nxs;
+        if (x < nx) {
+            const long long u = r * nx + x;
+            const double mu = m[u];
+            S[i] = (float)(dt2 / mu);
+            spo[i] = sp ? (float)sp[u] : 1.f;
+            vm[i] = v ? (float)(v[u] / mu) : 0.f;
+        } else {
+            S[i] = 0.f; spo[i] = 0.f; vm[i] = 0.f;
+        }
+    }
+}
+
+__global__ void k_wavelet(const double* __restrict__ w, float* o, int nt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nt) o[i] = (float)w[i];
+}
+
+__global__ void k_finalize(double* g, const double* __restrict__ m, double* grad, int nx, int nxs,
+                           long long ncp) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ncp;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % nxs);
+        const long long r = i / nxs;
+        if (x < nx) {
+            const long long u = r * nx + x;
+            grad[u] = g[i] / m[u];
+        }
+        g[i] = 0.0;
+    }
+}
+
+// Traces of receiver j = ordered sum of its slot samples (fwi.py:74-76); export
+// to the user layout, and build the adjoint source: mode 1 r = tr - dobs with
+// per-channel FP64 misfit partials, mode 2 r = tr (Born data), 0 none.
+__global__ void __launch_bounds__(256) k_gather(const float* __restrict__ rs, int nslot, int C, int logC,
+                                                int nt, int nrx, const int* __restrict__ rx_ptr,
+                                                int shot0, int nb, float* out,
+                                                const float* __restrict__ dobs, float* res,
+                                                int mode, double* jpart) {
+    __shared__ double sj[256];
+    const int tid = threadIdx.x;
+    const int c = tid & (C - 1);
+    const int rstep = 256 >> logC;
+    const long long rows = (long long)nt * nrx;
+    const long long per = (rows + gridDim.x - 1) / gridDim.x;
+    const long long r0 = blockIdx.x * per;
+    const long long r1 = min(rows, r0 + per);
+    double J = 0.0;
+    for (long long r = r0 + (tid >> logC); r < r1; r += rstep) {
+        const int n = (int)(r / nrx), j = (int)(r % nrx);
+        float tr = 0.f;
+        for (int e = rx_ptr[j]; e < rx_ptr[j + 1]; ++e) tr = tr + rs[((long long)n * nslot + e) * C + c];
+        if (c < nb) {
+            const long long uo = ((long long)(shot0 + c) * nt + n) * nrx + j;
+            if (out) out[uo] = tr;
+            if (mode == 1) {
+                const float rr = tr - dobs[uo];
+                res[r * C + c] = rr;
+                J += 0.5 * (double)rr * (double)rr;
+            } else if (mode == 2) {
+                res[r * C + c] = tr;
+            }
+        } else if (mode) {
+            res[r * C + c] = 0.f;
+        }
+    }
+    sj[tid] = J;
+    __syncthreads();
+    for (int s = 128; s >= C && s > 0; s >>= 1) {
+        if (tid < s) sj[tid] += sj[tid + s];
+        __syncthreads();
+    }
+    if (jpart && tid < C) jpart[blockIdx.x * C + tid] = sj[tid];
+}
+
+__global__ void k_jsum(const double* __restrict__ jpart, int C, int nblk, int shot0, int nb, double* J) {
+    const int c = threadIdx.x;
+    if (c < nb) {
+        double s = 0.0;
+        for (int b = 0; b < nblk; ++b) s += jpart[b * C + c];
+        J[shot0 + c] = s;
+    }
+}
+
+__global__ void k_adjsrc(const float* __restrict__ adj, float* res, int C, int nt, int nrx, int shot0,
+                         int nb) {
+    const long long tot = (long long)nt * nrx * C;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long r = i / C;
+        const int n = (int)(r / nrx), j = (int)(r % nrx);
+        res[i] = c < nb ? adj[((long long)(shot0 + c) * nt + n) * nrx + j] : 0.f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launches
+// ---------------------------------------------------------------------------
+static size_t stencil_smem(const usct_plan* p, int nfield) {
+    const int HF = p->C < 4 ? 4 : p->C;
+    return sizeof(float) * 2 * nfield * (p->ty + 2) * (4 * p->txv + 2 * HF);
+}
+
+template <bool BORN>
+static int launch_fwd(usct_plan* p, const FwdArgs& a, cudaStream_t s) {
+    const dim3 grid(p->ntx_t, p->nty_t, p->nzc);
+    const size_t smem = stencil_smem(p, BORN ? 2 : 1);
+    const int key = p->txv * 1000 + p->ty;
+    if (p->ndim == 3) {
+        switch (key) {
+            case 32004: k_forward<32, 4, true, BORN><<<grid, dim3(32, 4), smem, s>>>(a); break;
+            case 32008: k_forward<32, 8, true, BORN><<<grid, dim3(32, 8), smem, s>>>(a); break;
+            case 64002: k_forward<64, 2, true, BORN><<<grid, dim3(64, 2), smem, s>>>(a); break;
+            case 64004: k_forward<64, 4, true, BORN><<<grid, dim3(64, 4), smem, s>>>(a); break;
+            default: return set_err(USCT_ERR_ARG, "no 3D kernel for tile %d", key);
+        }
+    } else {
+        switch (key) {
+            case 64001: k_forward<64, 1, false, BORN><<<grid, dim3(64, 1), smem, s>>>(a); break;
+            case 128001: k_forward<128, 1, false, BORN><<<grid, dim3(128, 1), smem, s>>>(a); break;
+            default: return set_err(USCT_ERR_ARG, "no 2D kernel for tile %d", key);
+        }
+    }
+    ++p->launches;
+    CUDA_TRY(cudaGetLastError());
+    return USCT_OK;
+}
+
+static int launch_adj(usct_plan* p, const AdjArgs& a, cudaStream_t s) {
+    const dim3 grid(p->ntx_t, p->nty_t, p->nzc);
+    const size_t smem = stencil_smem(p, 1);
+    const int key = p->txv * 1000 + p->ty;
+    if (p->ndim == 3) {
+        switch (key) {
+            case 32004: k_adjoint<32, 4, true><<<grid, dim3(32, 4), smem, s>>>(a); break;
+            case 32008: k_adjoint<32, 8, true><<<grid, dim3(32, 8), smem, s>>>(a); break;
+            case 64002: k_adjoint<64, 2, true><<<grid, dim3(64, 2), smem, s>>>(a); break;
+            case 64004: k_adjoint<64, 4, true><<<grid, dim3(64, 4), smem, s>>>(a); break;
+            default: return set_err(USCT_ERR_ARG, "no 3D kernel for tile %d", key);
+        }
+    } else {
+        switch (key) {
+            case 64001: k_adjoint<64, 1, false><<<grid, dim3(64, 1), smem, s>>>(a); break;
+            case 128001: k_adjoint<128, 1, false><<<grid, dim3(128, 1), smem, s>>>(a); break;
+            default: return set_err(USCT_ERR_ARG, "no 2D kernel for tile %d", key);
+        }
+    }
+    ++p->launches;
+    CUDA_TRY(cudaGetLastError());
+    return USCT_OK;
+}
+
+static int grid1d(long long n, int bs = 256) {
+    long long g = (n + bs - 1) / bs;
+    return (int)std::max<long long>(1, std::min<long long>(g, 152LL * 32));
+}
+
+// ---------------------------------------------------------------------------
+// model
+// ---------------------------------------------------------------------------
+extern "C" int usct_model_prepare(usct_plan* p, void* model_ws, const double* m,
+                                  const double* sponge, const double* v, const double* wavelet,
+                                  void* stream) {
+    if (!p || !model_ws || !m || !wavelet) return set_err(USCT_ERR_ARG, "null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    ModelWS M = carve_model(p, model_ws);
+    const double dt2 = p->dt * p->dt;
+    k_prepare<<<grid1d((long long)p->cells_p), 256, 0, s>>>(m, sponge, v, M.S, M.sp, M.vm, dt2,
+                                                           p->geo.nx, p->geo.nxs,
+                                                           (long long)p->cells_p);
+    k_wavelet<<<(p->nt + 255) / 256, 256, 0, s>>>(wavelet, M.wav, p->nt);
+    p->launches += 2;
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemsetAsync(M.g, 0, p->cells_p * sizeof(double), s));
+    p->has_sp = sponge != nullptr;
+    p->has_vm = v != nullptr;
+    return USCT_OK;
+}
+
+extern "C" int usct_model_gradient(usct_plan* p, void* model_ws, const double* m, double* grad,
+                                   void* stream) {
+    if (!p || !model_ws || !m || !grad) return set_err(USCT_ERR_ARG, "null argument");
+    ModelWS M = carve_model(p, model_ws);
+    k_finalize<<<grid1d((long long)p->cells_p), 256, 0, (cudaStream_t)stream>>>(
+        M.g, m, grad, p->geo.nx, p->geo.nxs, (long long)p->cells_p);
+    ++p->launches;
+    CUDA_TRY(cudaGetLastError());
+    return USCT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batch sweeps
+// ---------------------------------------------------------------------------
+static int gather(usct_plan* p, const BatchWS& B, int b, float* out, const float* dobs, int mode,
+                  cudaStream_t s) {
+    const int shot0 = b * p->C;
+    const int nb = std::min(p->C, p->n_tx - shot0);
+    k_gather<<<JBLK, 256, 0, s>>>(B.rs, p->nslot, p->C, p->logC, p->nt, p->n_rx, p->d_rxptr, shot0,
+                                  nb, out, dobs, B.res, mode, B.jpart);
+    ++p->launches;
+    CUDA_TRY(cudaGetLastError());
+    return USCT_OK;
+}
+
+extern "C" int usct_batch_forward(usct_plan* p, const void* model_ws, void* batch_ws, int b,
+                                  int mode, float* traces, void* stream) {
+    if (!p || !model_ws || !batch_ws) return set_err(USCT_ERR_ARG, "null argument");
+    if (b < 0 || b >= p->nbatch) return set_err(USCT_ERR_ARG, "batch %d out of range", b);
+    if (mode < USCT_MODE_FORWARD || mode > USCT_MODE_BORN) return set_err(USCT_ERR_ARG, "bad mode");
+    if (mode == USCT_MODE_BORN && !p->has_vm)
+        return set_err(USCT_ERR_STATE, "Born sweep needs a model prepared with v");
+    cudaStream_t s = (cudaStream_t)stream;
+    const ModelWS M = carve_model(p, (void*)model_ws);
+    const BatchWS B = carve_batch(p, batch_ws, mode);
+    const size_t lvb = al256(p->LV * sizeof(float));
+    CUDA_TRY(cudaMemsetAsync(B.P[0], 0, 2 * lvb, s));
+    CUDA_TRY(cudaMemsetAsync(B.rs, 0, (size_t)p->nslot * p->C * sizeof(float), s));
+    if (mode == USCT_MODE_BORN) CUDA_TRY(cudaMemsetAsync(B.D[0], 0, 2 * lvb, s));
+    if (mode >= USCT_MODE_GRADIENT) CUDA_TRY(cudaMemsetAsync(B.ck, 0, 2 * lvb, s));
+    const size_t lvf = lvb / sizeof(float);
+    const int k = p->k, nt = p->nt;
+    const int al = (p->nseg - 1) * k;
+    for (int n = 1; n < nt; ++n) {
+        FwdArgs a{};
+        a.g = p->geo;
+        a.pc = B.P[(n - 1) & 1];
+        a.pp = B.P[n & 1];
+        a.pn = B.P[n & 1];
+        a.S = M.S;
+        a.sp = p->has_sp ? M.sp : nullptr;
+        a.wav = M.wav;
+        a.n = n;
+        if (mode >= USCT_MODE_GRADIENT) {
+            if ((n + 1) % k == 0 && n + 1 < nt - 1) a.ck = B.ck + (size_t)((n + 1) / k) * 2 * lvf;
+            else if (n % k == 0 && n < nt - 1) a.ck = B.ck + ((size_t)(n / k) * 2 + 1) * lvf;
+            if (n > al) a.d2 = B.stash + (size_t)(n - al - 1) * lvf;
+        }
+        a.s_ptr = p->d_sptr + (size_t)b * (p->ntiles + 1);
+        a.s_ent = p->d_sent;
+        a.r_ptr = p->d_rptr;
+        a.r_ent = p->d_rent;
+        a.rs = B.rs + (size_t)n * p->nslot * p->C;
+        if (mode == USCT_MODE_BORN) {
+            a.dc = B.D[(n - 1) & 1];
+            a.dpp = B.D[n & 1];
+            a.dn = B.D[n & 1];
+            a.vm = M.vm;
+            TRY(launch_fwd<true>(p, a, s));
+        } else {
+            TRY(launch_fwd<false>(p, a, s));
+        }
+    }
+    return gather(p, B, b, traces, nullptr, mode == USCT_MODE_BORN ? 2 : 0, s);
+}
+
+extern "C" int usct_batch_misfit(usct_plan* p, void* batch_ws, int b, const float* dobs, double* J,
+                                 void* stream) {
+    if (!p || !batch_ws || !dobs) return set_err(USCT_ERR_ARG, "null argument");
+    if (b < 0 || b >= p->nbatch) return set_err(USCT_ERR_ARG, "batch %d out of range", b);
+    cudaStream_t s = (cudaStream_t)stream;
+    const BatchWS B = carve_batch(p, batch_ws, USCT_MODE_FORWARD);
+    TRY(gather(p, B, b, nullptr, dobs, 1, s));
+    if (J) {
+        const int shot0 = b * p->C;
+        const int nb = std::min(p->C, p->n_tx - shot0);
+        k_jsum<<<1, 64, 0, s>>>(B.jpart, p->C, JBLK, shot0, nb, J);
+        ++p->launches;
+        CUDA_TRY(cudaGetLastError());
+    }
+    return USCT_OK;
+}
+
+extern "C" int usct_batch_adjoint_source(usct_plan* p, void* batch_ws, int b, const float* adj,
+                                         void* stream) {
+    if (!p || !batch_ws || !adj) return set_err(USCT_ERR_ARG, "null argument");
+    if (b < 0 || b >= p->nbatch) return set_err(USCT_ERR_ARG, "batch %d out of range", b);
+    const BatchWS B = carve_batch(p, batch_ws, USCT_MODE_FORWARD);
+    const int shot0 = b * p->C;
+    const int nb = std::min(p->C, p->n_tx - shot0);
+    k_adjsrc<<<grid1d((long long)p->nt * p->n_rx * p->C), 256, 0, (cudaStream_t)stream>>>(
+        adj, B.res, p->C, p->nt, p->n_rx, shot0, nb);
+    ++p->launches;
+    CUDA_TRY(cudaGetLastError());
+    return USCT_OK;
+}
+
+extern "C" int usct_batch_backward(usct_plan* p, void* model_ws, void* batch_ws, int b, void* stream) {
+    if (!p || !model_ws || !batch_ws) return set_err(USCT_ERR_ARG, "null argument");
+    if (b < 0 || b >= p->nbatch) return set_err(USCT_ERR_ARG, "batch %d out of range", b);
+    cudaStream_t s = (cudaStream_t)stream;
+    const ModelWS M = carve_model(p, model_ws);
+    const BatchWS B = carve_batch(p, batch_ws, USCT_MODE_GRADIENT);
+    const size_t lvb = al256(p->LV * sizeof(float));
+    const size_t lvf = lvb / sizeof(float);
+    CUDA_TRY(cudaMemsetAsync(B.L[0], 0, 2 * lvb, s));
+    const int k = p->k, nt = p->nt;
+    float* W[2] = {B.P[0], B.P[1]};
+    for (int j = p->nseg - 1; j >= 0; --j) {
+        const int a0 = j * k;
+        const int b1 = std::min(a0 + k, nt - 1);
+        const float* ck0 = B.ck + (size_t)j * 2 * lvf;
+        const float* ck1 = ck0 + lvf;
+        if (j != p->nseg - 1) {
+            for (int n = a0 + 1; n <= b1; ++n) {
+                FwdArgs a{};
+                a.g = p->geo;
+                a.pc = (n == a0 + 1) ? ck1 : W[(n - 1) & 1];
+                a.pp = (n == a0 + 1) ? ck0 : (n == a0 + 2 ? ck1 : W[n & 1]);
+                a.pn = W[n & 1];
+                a.S = M.S;
+                a.sp = p->has_sp ? M.sp : nullptr;
+                a.wav = M.wav;
+                a.n = n;
+                a.d2 = B.stash + (size_t)(n - a0 - 1) * lvf;
+                a.s_ptr = p->d_sptr + (size_t)b * (p->ntiles + 1);
+                a.s_ent = p->d_sent;
+                a.r_ptr = p->d_rptr;
+                a.r_ent = p->d_rent;
+                TRY(launch_fwd<false>(p, a, s));
+            }
+        }
+        for (int kk = b1; kk >= a0 + 1; --kk) {
+            AdjArgs a{};
+            a.g = p->geo;
+            a.l1 = B.L[(kk + 1) & 1];
+            a.l2 = B.L[kk & 1];
+            a.lk = B.L[kk & 1];
+            a.S = M.S;
+            a.sp = p->has_sp ? M.sp : nullptr;
+            a.d2 = B.stash + (size_t)(kk - a0 - 1) * lvf;
+            a.gacc = M.g;
+            a.r_ptr = p->d_rptr;
+            a.r_ent = p->d_rent;
+            a.res = B.res + (size_t)kk * p->n_rx * p->C;
+            TRY(launch_adj(p, a, s));
+        }
+    }
+    return USCT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// whole-acquisition device calls
+// ---------------------------------------------------------------------------
+extern "C" int usct_forward_fmc_dev(usct_plan* p, const double* m, const double* sponge,
+                                    const double* wavelet, float* data, void* model_ws,
+                                    void* batch_ws, void* stream) {
+    TRY(usct_model_prepare(p, model_ws, m, sponge, nullptr, wavelet, stream));
+    for (int b = 0; b < p->nbatch; ++b)
+        TRY(usct_batch_forward(p, model_ws, batch_ws, b, USCT_MODE_FORWARD, data, stream));
+    return USCT_OK;
+}
+
+extern "C" int usct_misfit_and_gradient_dev(usct_plan* p, const double* m, const double* sponge,
+                                            const double* wavelet, const float* dobs, double* J,
+                                            double* grad, void* model_ws, void* batch_ws,
+                                            void* stream) {
+    TRY(usct_model_prepare(p, model_ws, m, sponge, nullptr, wavelet, stream));
+    for (int b = 0; b < p->nbatch; ++b) {
+        TRY(usct_batch_forward(p, model_ws, batch_ws, b, USCT_MODE_GRADIENT, nullptr, stream));
+        TRY(usct_batch_misfit(p, batch_ws, b, dobs, J, stream));
+        TRY(usct_batch_backward(p, model_ws, batch_ws, b, stream));
+    }
+    return usct_model_gradient(p, model_ws, m, grad, stream);
+}
+
+extern "C" int usct_gn_hessian_vector_dev(usct_plan* p, const double* m, const double* sponge,
+                                          const double* wavelet, const double* v, double* hv,
+                                          float* born, void* model_ws, void* batch_ws,
+                                          void* stream) {
+    if (!v) return set_err(USCT_ERR_ARG, "v is null");
+    TRY(usct_model_prepare(p, model_ws, m, sponge, v, wavelet, stream));
+    for (int b = 0; b < p->nbatch; ++b) {
+        TRY(usct_batch_forward(p, model_ws, batch_ws, b, USCT_MODE_BORN, born, stream));
+        TRY(usct_batch_backward(p, model_ws, batch_ws, b, stream));
+    }
+    return usct_model_gradient(p, model_ws, m, hv, stream);
+}
+
+// ---------------------------------------------------------------------------
+// host-pointer calls with the reference core's signatures
+// ---------------------------------------------------------------------------
+namespace {
+struct DevBuf {
+    void* p = nullptr;
+    ~DevBuf() { if (p) cudaFree(p); }
+};
+}  // namespace
+
+static int host_plan(usct_plan** plan, const int* dims, int ndim, double h, double dt, int nt,
+                     const int* tx_lin, int n_tx, const int* rec_lin, int n_rec) {
+    if (!tx_lin || !rec_lin) return set_err(USCT_ERR_ARG, "null index array");
+    std::vector<int> tp(n_tx + 1), rp(n_rec + 1);
+    std::vector<int64_t> tc(n_tx), rc(n_rec);
+    std::vector<double> tw(n_tx, 1.0), rw(n_rec, 1.0);
+    for (int i = 0; i <= n_tx; ++i) tp[i] = i;
+    for (int i = 0; i <= n_rec; ++i) rp[i] = i;
+    for (int i = 0; i < n_tx; ++i) tc[i] = tx_lin[i];
+    for (int i = 0; i < n_rec; ++i) rc[i] = rec_lin[i];
+    return usct_plan_create(plan, ndim, dims, h, dt, nt, n_tx, tp.data(), tc.data(), tw.data(), n_rec,
+                            rp.data(), rc.data(), rw.data(), 0, 0, 0, 0, 0);
+}
+
+extern "C" int usct_forward_fmc(const double* m, const int* dims, int ndim, double h, double dt, int nt,
+                                const int* tx_lin, int n_tx, const int* rec_lin, int n_rec,
+                                const double* wavelet, double* data) {
+    if (!m || !wavelet || !data) return set_err(USCT_ERR_ARG, "null argument");
+    usct_plan* p = nullptr;
+    TRY(host_plan(&p, dims, ndim, h, dt, nt, tx_lin, n_tx, rec_lin, n_rec));
+    struct Guard { usct_plan* p; ~Guard() { usct_plan_destroy(p); } } guard{p};
+    const size_t nd = (size_t)n_tx * nt * n_rec;
+    DevBuf dm, dw, dd, mws, bws;
+    CUDA_TRY(cudaMalloc(&dm.p, p->N * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&dw.p, (size_t)nt * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&dd.p, nd * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&mws.p, usct_model_bytes(p)));
+    CUDA_TRY(cudaMalloc(&bws.p, usct_batch_bytes(p, USCT_MODE_FORWARD)));
+    CUDA_TRY(cudaMemcpy(dm.p, m, p->N * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dw.p, wavelet, (size_t)nt * sizeof(double), cudaMemcpyHostToDevice));
+    TRY(usct_forward_fmc_dev(p, (const double*)dm.p, nullptr, (const double*)dw.p, (float*)dd.p,
+                             mws.p, bws.p, nullptr));
+    std::vector<float> hf(nd);
+    CUDA_TRY(cudaMemcpy(hf.data(), dd.p, nd * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < nd; ++i) data[i] = hf[i];
+    return USCT_OK;
+}
+
+extern "C" int usct_misfit_and_gradient(const double* m, const int* dims, int ndim, double h,
+                                        double dt, int nt, const int* tx_lin, int n_tx,
+                                        const int* rec_lin, int n_rec, const double* wavelet,
+                                        const double* dobs, double* grad, double* J) {
+    if (!m || !wavelet || !dobs || !grad) return set_err(USCT_ERR_ARG, "null argument");
+    usct_plan* p = nullptr;
+    TRY(host_plan(&p, dims, ndim, h, dt, nt, tx_lin, n_tx, rec_lin, n_rec));
+    struct Guard { usct_plan* p; ~Guard() { usct_plan_destroy(p); } } guard{p};
+    const size_t nd = (size_t)n_tx * nt * n_rec;
+    std::vector<float> hdobs(nd);
+    for (size_t i = 0; i < nd; ++i) hdobs[i] = (float)dobs[i];
+    DevBuf dm, dw, dob, dJ, dg, mws, bws;
+    CUDA_TRY(cudaMalloc(&dm.p, p->N * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&dw.p, (size_t)nt * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&dob.p, nd * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&dJ.p, (size_t)n_tx * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&dg.p, p->N * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&mws.p, usct_model_bytes(p)));
+    CUDA_TRY(cudaMalloc(&bws.p, usct_batch_bytes(p, USCT_MODE_GRADIENT)));
+    CUDA_TRY(cudaMemcpy(dm.p, m, p->N * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dw.p, wavelet, (size_t)nt * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dob.p, hdobs.data(), nd * sizeof(float), cudaMemcpyHostToDevice));
+    TRY(usct_misfit_and_gradient_dev(p, (const double*)dm.p, nullptr, (const double*)dw.p,
+                                     (const float*)dob.p, (double*)dJ.p, (double*)dg.p, mws.p,
+                                     bws.p, nullptr));
+    std::vector<double> hJ(n_tx);
+    CUDA_TRY(cudaMemcpy(hJ.data(), dJ.p, (size_t)n_tx * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(grad, dg.p, p->N * sizeof(double), cudaMemcpyDeviceToHost));
+    if (J) {
+        double s = 0.0;
+        for (int t = 0; t < n_tx; ++t) s += hJ[t];
+        *J = s;
+    }
+    return USCT_OK;
+}
+
+// The plain one-shot-per-launch form needs the plan internals declared above.
+#include "usct_plain.cuh"

@@ -1,0 +1,197 @@
+"""Acquisition geometry on the finite-difference grid (host side).
+
+The engine consumes elements as CSR lists of (row-major linear cell, weight).
+``element_csr`` builds them from the reference's own geometry objects (anything
+with an ``idx`` list of grid-index tuples -- ``RingArray``, ``CylinderArray``,
+``GridArray`` in simulation/ringfwi/geometry.py) and, optionally, from the
+finite-aperture footprints of ``build_footprints`` (geometry.py:212-278).
+
+``RingGeometry`` / ``CylinderGeometry`` place elements exactly as the
+reference's ``RingArray.__post_init__`` (geometry.py:39-50) and
+``CylinderArray.__post_init__`` (geometry.py:103-123) do, for hosts where the
+reference package is not installed; ``ricker`` is the wavelet of
+simulation/ringfwi/sources.py:8-26.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+def linear_indices(idx, shape) -> np.ndarray:
+    """Row-major linear indices of grid-index tuples (software/python/uap.py:19-22)."""
+    idx = np.asarray(idx, dtype=np.int64).reshape(len(idx), -1)
+    if idx.shape[1] != len(shape):
+        raise ValueError(f"element indices have {idx.shape[1]} axes, grid has {len(shape)}")
+    if np.any(idx < 0) or np.any(idx >= np.asarray(shape)[None, :]):
+        raise ValueError("element index outside the grid")
+    strides = np.cumprod((1,) + tuple(int(s) for s in shape[::-1][:-1]))[::-1]
+    return (idx * strides[None, :]).sum(axis=1).astype(np.int64)
+
+
+@dataclass
+class CSR:
+    ptr: np.ndarray    # int32 [rows+1]
+    cell: np.ndarray   # int64 [entries]
+    w: np.ndarray      # float64 [entries]
+
+    @property
+    def rows(self) -> int:
+        return len(self.ptr) - 1
+
+    def key(self) -> bytes:
+        return self.ptr.tobytes() + b"|" + self.cell.tobytes() + b"|" + self.w.tobytes()
+
+
+def _groups_csr(groups, shape) -> CSR:
+    ptr = [0]
+    cells, ws = [], []
+    for idxs, w in groups:
+        lin = linear_indices(list(idxs), shape)
+        w = np.asarray(w, dtype=np.float64).reshape(-1)
+        if len(w) != len(lin):
+            raise ValueError("footprint weights and cells differ in length")
+        cells.append(lin)
+        ws.append(w)
+        ptr.append(ptr[-1] + len(lin))
+    return CSR(np.asarray(ptr, np.int32),
+               np.concatenate(cells) if cells else np.zeros(0, np.int64),
+               np.concatenate(ws) if ws else np.zeros(0, np.float64))
+
+
+def element_csr(geom, shape, src_list=None, footprints=None):
+    """Transmit and receive CSR lists for ``forward_fmc`` semantics.
+
+    Every listed element transmits in turn and all elements receive
+    (fwi.py:109-118); with ``footprints`` each element is its aperture's cell
+    list with weights summing to one, on transmit and on receive (fwi.py:84-89,
+    74-76), otherwise a single cell of weight 1.
+    """
+    idx = list(geom.idx) if hasattr(geom, "idx") else list(geom)
+    n_el = len(idx)
+    if footprints is None:
+        groups = [([t], [1.0]) for t in idx]
+    else:
+        if len(footprints) != n_el:
+            raise ValueError("one footprint per element is required")
+        groups = [(list(c), list(w)) for c, w in footprints]
+    if src_list is None:
+        src_list = list(range(n_el))
+    src_list = [int(s) for s in src_list]
+    for s in src_list:
+        if not 0 <= s < n_el:
+            raise ValueError(f"src_list entry {s} outside 0..{n_el - 1}")
+    rx = _groups_csr(groups, shape)
+    tx = _groups_csr([groups[s] for s in src_list], shape)
+    return tx, rx
+
+
+# ---------------------------------------------------------------------------
+# element placement (same formulas as the reference geometry classes)
+# ---------------------------------------------------------------------------
+@dataclass
+class RingGeometry:
+    """Planar ring of ``n_elements`` on a square grid (RingArray semantics)."""
+
+    n_elements: int
+    radius_m: float
+    domain_m: float
+    h: float
+    idx: list = field(init=False)
+    n: int = field(init=False)
+    array_type = "ring"
+
+    def __post_init__(self):
+        self.n = int(round(self.domain_m / self.h)) + 1
+        c = self.domain_m / 2.0
+        ang = np.linspace(0.0, 2.0 * np.pi, self.n_elements, endpoint=False)
+        self.xy = np.column_stack([c + self.radius_m * np.cos(ang), c + self.radius_m * np.sin(ang)])
+        self.idx = [(int(round(y / self.h)), int(round(x / self.h))) for x, y in self.xy]
+
+    @property
+    def grid_shape(self):
+        return (self.n, self.n)
+
+    def element_index(self, k):
+        return self.idx[k]
+
+    @property
+    def element_positions(self):
+        return self.xy - self.domain_m / 2.0
+
+
+@dataclass
+class CylinderGeometry:
+    """Rings stacked along z on a cubic grid (CylinderArray semantics)."""
+
+    n_rings: int
+    per_ring: int
+    radius_m: float
+    height_m: float
+    domain_m: float
+    h: float
+    idx: list = field(init=False)
+    n: int = field(init=False)
+    array_type = "cylinder"
+
+    def __post_init__(self):
+        self.n = int(round(self.domain_m / self.h)) + 1
+        c = self.domain_m / 2.0
+        if self.n_rings == 1:
+            zs = np.array([c])
+        else:
+            zs = c + np.linspace(-self.height_m / 2.0, self.height_m / 2.0, self.n_rings)
+        ang = np.linspace(0.0, 2.0 * np.pi, self.per_ring, endpoint=False)
+        xyz = [[c + self.radius_m * np.cos(a), c + self.radius_m * np.sin(a), z] for z in zs for a in ang]
+        self.xyz = np.asarray(xyz)
+        self.idx = [(int(round(z / self.h)), int(round(y / self.h)), int(round(x / self.h)))
+                    for x, y, z in self.xyz]
+
+    @property
+    def n_elements(self):
+        return len(self.idx)
+
+    @property
+    def grid_shape(self):
+        return (self.n, self.n, self.n)
+
+    def element_index(self, k):
+        return self.idx[k]
+
+    @property
+    def element_positions(self):
+        return self.xyz - self.domain_m / 2.0
+
+
+@dataclass
+class IndexGeometry:
+    """Elements given directly as grid-index tuples (GridArray semantics)."""
+
+    idx: list
+
+    @property
+    def n_elements(self):
+        return len(self.idx)
+
+    def element_index(self, k):
+        return self.idx[k]
+
+
+def footprints_from_csr(ptr, cells, w):
+    """(idx_list, weights) list from a CSR of grid-index tuples."""
+    out = []
+    for a, b in zip(ptr[:-1], ptr[1:]):
+        out.append(([tuple(int(v) for v in c) for c in cells[a:b]], np.asarray(w[a:b], float)))
+    return out
+
+
+def ricker(nt, dt, f0, t0=None):
+    """Ricker wavelet (1 - 2a) exp(-a), a = (pi f0 (t - t0))^2, t0 = 1/f0."""
+    if t0 is None:
+        t0 = 1.0 / f0
+    t = np.arange(nt) * dt - t0
+    a = (math.pi * f0 * t) ** 2
+    return (1.0 - 2.0 * a) * np.exp(-a)

@@ -1,0 +1,196 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Run in a container that has the reference checkout (it is not needed anywhere
+else; the fixtures are committed):
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+Every case is computed by the reference's Python package ``ringfwi``
+(``simulation/ringfwi/fwi.py``) and, for point elements, also by the
+reference's own C++ core ``software/core/libuap.hpp`` (compiled by
+``oracle/Makefile`` into ``oracle/_ref/``).  The setups mirror the reference's
+own tests:
+
+* ring2d_point    -- simulation/tests/test_gradient.py:20-40
+* ring2d_aperture -- simulation/tests/test_gradient_aperture.py:161-180
+* ring2d_sponge   -- test_gradient.py setup with solver.make_sponge(width=6)
+* gn2d            -- simulation/tests/test_gauss_newton.py:234-246
+* cyl3d_point     -- simulation/tests/test_gradient_3d.py:94-113
+* cyl3d_aperture  -- test_gradient_3d.py setup with build_footprints(rect)
+* odd2d / odd3d   -- non-square grids with GridArray elements, one element on
+                     the grid border (exercises the lap = 0 border rule)
+* parity2d/parity3d -- software/python/test_parity.py:76-90 (the reference's
+                     C++-vs-Python parity problems)
+* gpu3d           -- software/python/test_gpu.py:139-152 (the reference's
+                     FP32-GPU-vs-FP64 parity problem, every third element)
+
+Each fixture stores the inputs (m, m0, element indices, footprints as CSR,
+wavelet, dt, h, nt, src_list, sponge) and the reference outputs (dobs, J, g,
+and Hv for the Gauss-Newton cases).
+"""
+
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+
+def _fp_csr(footprints):
+    ptr, cells, w = [0], [], []
+    for idxs, ws in footprints:
+        for c, wi in zip(idxs, ws):
+            cells.append(tuple(int(a) for a in c))
+            w.append(float(wi))
+        ptr.append(len(cells))
+    return np.asarray(ptr, np.int32), np.asarray(cells, np.int32), np.asarray(w)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    sys.path.insert(0, os.path.join(args.ref, "simulation"))
+    sys.path.insert(0, REPO)
+    from ringfwi import fwi, phantom
+    from ringfwi.geometry import CylinderArray, GridArray, RingArray, build_footprints
+    from ringfwi.solver import make_sponge
+    from ringfwi.sources import ricker
+
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref",
+                    f"REF={args.ref}"], check=True)
+    import oracle
+
+    def save(name, **kw):
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **kw)
+        print(f"wrote {path} ({os.path.getsize(path)} B)")
+
+    def point_case(name, geom, m_true, m0, wav, dt, h, nt, src_list, sponge=None,
+                   with_cpp=True):
+        idx = np.asarray(geom.idx, np.int32)
+        dobs = fwi.forward_fmc(m_true, geom, wav, dt, h, nt, sponge, src_list)
+        J, g = fwi.misfit_and_gradient(m0, geom, wav, dt, h, nt, dobs, sponge, src_list)
+        out = dict(m_true=m_true, m0=m0, idx=idx, wavelet=wav, dt=dt, h=h, nt=nt,
+                   src_list=np.asarray(src_list, np.int32), dobs=dobs, J=J, g=g,
+                   sponge=np.zeros(0) if sponge is None else sponge)
+        if with_cpp:
+            out["dobs_cpp"] = oracle.ref_forward_fmc(m_true, geom, wav, dt, h, nt, src_list)
+            Jc, gc = oracle.ref_misfit_and_gradient(m0, geom, wav, dt, h, nt, dobs, src_list)
+            out["J_cpp"] = Jc
+            out["g_cpp"] = gc
+            assert np.abs(out["dobs_cpp"] - dobs).max() <= 1e-12 * np.abs(dobs).max()
+            assert abs(Jc - J) <= 1e-12 * abs(J)
+        save(name, **out)
+
+    # --- 2D ring, point elements (test_gradient.py) ---------------------------
+    h = 1.0e-3
+    geom = RingArray(n_elements=8, radius_m=0.024, domain_m=0.06, h=h)
+    n = geom.n
+    dt, nt = 1.2e-7, 350
+    wav = ricker(nt, dt, 0.4e6)
+    c0 = phantom.coupling_background((n, n), 3000.0, 1480.0, 0.02, h)
+    ct = phantom.add_inclusion(c0, (0.5, 0.5), 0.006, 3400.0, h)
+    m_true, m0 = phantom.velocity_to_m(ct), phantom.velocity_to_m(c0)
+    point_case("ring2d_point", geom, m_true, m0, wav, dt, h, nt, [0, 4])
+
+    # --- 2D sponge (fwi.py:68-69, 313-314) ------------------------------------
+    sp = make_sponge((n, n), width=6)
+    point_case("ring2d_sponge", geom, m_true, m0, wav, dt, h, nt, [0, 4], sponge=sp,
+               with_cpp=False)
+
+    # --- 2D finite aperture (test_gradient_aperture.py) -----------------------
+    fps = build_footprints(geom, width_m=0.003, shape="flat")
+    dobs = fwi.forward_fmc(m_true, geom, wav, dt, h, nt, src_list=[0, 4], footprints=fps)
+    J, g = fwi.misfit_and_gradient(m0, geom, wav, dt, h, nt, dobs, src_list=[0, 4],
+                                   footprints=fps)
+    fp_ptr, fp_idx, fp_w = _fp_csr(fps)
+    save("ring2d_aperture", m_true=m_true, m0=m0, idx=np.asarray(geom.idx, np.int32),
+         wavelet=wav, dt=dt, h=h, nt=nt, src_list=np.asarray([0, 4], np.int32), dobs=dobs,
+         J=J, g=g, fp_ptr=fp_ptr, fp_idx=fp_idx, fp_w=fp_w, sponge=np.zeros(0))
+
+    # --- 2D Gauss-Newton Hv (test_gauss_newton.py) ----------------------------
+    nt_gn = 300
+    wav_gn = ricker(nt_gn, dt, 0.4e6)
+    rng = np.random.default_rng(2)
+    v = rng.standard_normal((n, n))
+    v[:5] = v[-5:] = v[:, :5] = v[:, -5:] = 0.0
+    v *= float(np.mean(m0))
+    Hv = fwi.gn_hessian_vector(m0, geom, wav_gn, dt, h, nt_gn, v, src_list=[0, 4])
+    save("gn2d", m0=m0, idx=np.asarray(geom.idx, np.int32), wavelet=wav_gn, dt=dt, h=h,
+         nt=nt_gn, src_list=np.asarray([0, 4], np.int32), v=v, Hv=Hv, sponge=np.zeros(0))
+
+    # --- 3D cylinder, point elements (test_gradient_3d.py) ---------------------
+    h3 = 1.5e-3
+    cyl = CylinderArray(n_rings=2, per_ring=6, radius_m=0.010, height_m=0.012,
+                        domain_m=0.03, h=h3)
+    n3 = cyl.n
+    dt3, nt3 = 1.5e-7, 140
+    wav3 = ricker(nt3, dt3, 0.35e6)
+    c3 = phantom.cylinder_background((n3, n3, n3), 3000.0, 1480.0, 0.008, h3)
+    ct3 = phantom.add_sphere(c3, (0.5, 0.5, 0.5), 0.004, 2700.0, h3)
+    point_case("cyl3d_point", cyl, phantom.velocity_to_m(ct3), phantom.velocity_to_m(c3),
+               wav3, dt3, h3, nt3, [0, 6])
+
+    # --- 3D finite aperture (rect footprints) ---------------------------------
+    fps3 = build_footprints(cyl, width_m=0.004, shape="rect", height_m=0.003)
+    mt3, m03 = phantom.velocity_to_m(ct3), phantom.velocity_to_m(c3)
+    dobs3 = fwi.forward_fmc(mt3, cyl, wav3, dt3, h3, nt3, src_list=[0, 6], footprints=fps3)
+    J3, g3 = fwi.misfit_and_gradient(m03, cyl, wav3, dt3, h3, nt3, dobs3, src_list=[0, 6],
+                                     footprints=fps3)
+    fp_ptr, fp_idx, fp_w = _fp_csr(fps3)
+    save("cyl3d_aperture", m_true=mt3, m0=m03, idx=np.asarray(cyl.idx, np.int32),
+         wavelet=wav3, dt=dt3, h=h3, nt=nt3, src_list=np.asarray([0, 6], np.int32),
+         dobs=dobs3, J=J3, g=g3, fp_ptr=fp_ptr, fp_idx=fp_idx, fp_w=fp_w,
+         sponge=np.zeros(0))
+
+    # --- odd, non-square grids with an element on the border -------------------
+    rs = np.random.default_rng(7)
+    shp2 = (37, 53)
+    idx2 = [(int(rs.integers(3, shp2[0] - 3)), int(rs.integers(3, shp2[1] - 3)))
+            for _ in range(5)] + [(0, 20), (36, 52)]
+    g2 = GridArray(idx=idx2, n=shp2[0], h=1.0e-3, radius_m=0.015, domain_m=0.036)
+    c2 = 1500.0 + 60.0 * rs.standard_normal(shp2)
+    point_case("odd2d", g2, phantom.velocity_to_m(c2), phantom.velocity_to_m(np.full(shp2, 1500.0)),
+               ricker(200, 1.5e-7, 0.35e6), 1.5e-7, 1.0e-3, 200, [0, 3, 5, 6])
+
+    # --- the reference's own parity problems (test_parity.py, test_gpu.py) ----
+    ring16 = RingArray(n_elements=16, radius_m=0.024, domain_m=0.060, h=6e-4)
+    n16 = ring16.n
+    cp2 = phantom.coupling_background((n16, n16), 3000.0, 1480.0, 0.020, 6e-4)
+    cp2 = phantom.add_inclusion(cp2, (0.58, 0.46), 0.006, 2650.0, 6e-4)
+    point_case("parity2d", ring16, phantom.velocity_to_m(cp2),
+               phantom.velocity_to_m(np.full((n16, n16), np.mean(cp2))),
+               ricker(500, 7e-8, 0.3e6), 7e-8, 6e-4, 500, list(range(16)))
+    cylp = CylinderArray(n_rings=3, per_ring=12, radius_m=0.015, height_m=0.014,
+                         domain_m=0.036, h=1.25e-3)
+    npc = cylp.n
+    cp3 = phantom.cylinder_background((npc, npc, npc), 3000.0, 1480.0, 0.012, 1.25e-3)
+    cp3 = phantom.add_sphere(cp3, (0.56, 0.5, 0.5), 0.005, 2650.0, 1.25e-3)
+    point_case("parity3d", cylp, phantom.velocity_to_m(cp3),
+               phantom.velocity_to_m(np.full((npc, npc, npc), np.mean(cp3))),
+               ricker(250, 1.2e-7, 0.3e6), 1.2e-7, 1.25e-3, 250, list(range(0, 36, 4)))
+    cg3 = phantom.cylinder_background((npc, npc, npc), 3000.0, 1480.0, 0.015 * 0.8, 1.25e-3)
+    cg3 = phantom.add_sphere(cg3, (0.56, 0.5, 0.5), 0.005, 2650.0, 1.25e-3)
+    point_case("gpu3d", cylp, phantom.velocity_to_m(cg3),
+               phantom.velocity_to_m(np.full((npc, npc, npc), 3000.0)),
+               ricker(250, 1.2e-7, 0.3e6), 1.2e-7, 1.25e-3, 250, list(range(0, 36, 3)))
+
+    shp3 = (13, 17, 21)
+    idx3 = [(int(rs.integers(2, shp3[0] - 2)), int(rs.integers(2, shp3[1] - 2)),
+             int(rs.integers(2, shp3[2] - 2))) for _ in range(5)] + [(0, 8, 10), (6, 16, 3)]
+    g3d = GridArray(idx=idx3, n=shp3[0], h=1.0e-3, radius_m=0.008, domain_m=0.02)
+    c3d = 1500.0 + 60.0 * rs.standard_normal(shp3)
+    point_case("odd3d", g3d, phantom.velocity_to_m(c3d),
+               phantom.velocity_to_m(np.full(shp3, 1500.0)), ricker(120, 1.5e-7, 0.35e6),
+               1.5e-7, 1.0e-3, 120, [0, 2, 5, 6])
+
+
+if __name__ == "__main__":
+    main()

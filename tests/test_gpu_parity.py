@@ -1,0 +1,222 @@
+"""GPU parity: the CUDA path against the oracle on the committed goldens.
+
+* bit for bit against the FP32 kernel-order restatement (oracle o32_*), for
+  several shot-batch widths and launch shapes -- this pins indexing, halos,
+  the shot-innermost layout, source/receiver entries and the shot reduction;
+* within the FP32 tolerances (golden_util.TRACE_TOL / GRAD_TOL) of the
+  reference's FP64 outputs;
+* checkpoint recompute bit-identical to no recompute;
+* batched shots bit-identical to one shot per launch.
+All calls go through the C ABI (libusct_gb300.so) via the backend module.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from golden_util import CASES, grad_tol, load, rel_l2, rel_max, trace_tol
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def cuda():
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    from openusct_gb300 import build
+    build.build()
+    yield
+
+
+def gb():
+    import openusct_gb300.backend as backend
+    return backend
+
+
+def _tiles(ndim):
+    return [(32, 4, 0), (32, 8, 3), (64, 2, 5), (64, 4, 0)] if ndim == 3 else [(64, 1, 0),
+                                                                               (128, 1, 7)]
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("C", [1, 2, 4])
+def test_forward_bit_exact_vs_fp32_restatement(name, C):
+    c = load(name)
+    a = c.args()
+    ref = oracle.forward_fmc32(c["m_true"], c.geom, a["wavelet"], c.dt, c.h, c.nt, a["sponge"],
+                               a["src_list"], a["footprints"])
+    for tile in _tiles(c["m_true"].ndim)[: 1 if C != 2 else None]:
+        d = gb().forward_fmc(torch.from_numpy(c["m_true"]).cuda(), c.geom, a["wavelet"], c.dt,
+                             c.h, c.nt, a["sponge"], a["src_list"], a["footprints"], batch=C,
+                             tile=tile)
+        d = d.cpu().numpy()
+        assert d.dtype == np.float32
+        assert np.array_equal(d, ref), f"tile {tile}: max diff {np.abs(d - ref).max()}"
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_forward_vs_reference_fp64(name):
+    c = load(name)
+    a = c.args()
+    d = gb().forward_fmc(c["m_true"], c.geom, a["wavelet"], c.dt, c.h, c.nt, a["sponge"],
+                         a["src_list"], a["footprints"])
+    assert d.dtype == np.float64 and d.shape == c["dobs"].shape
+    assert rel_l2(d, c["dobs"]) < trace_tol(name)
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("C", [1, 4])
+def test_gradient_bit_exact_vs_fp32_restatement(name, C):
+    c = load(name)
+    a = c.args()
+    Jr, gr = oracle.misfit_and_gradient32(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt,
+                                          c["dobs"], a["sponge"], a["src_list"], a["footprints"],
+                                          C=C)
+    J, g, Js = gb().misfit_and_gradient(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt,
+                                        c["dobs"], a["sponge"], a["src_list"],
+                                        footprints=a["footprints"], batch=C, ckpt_k=5,
+                                        return_per_shot=True)
+    assert np.allclose(Js, Jr, rtol=1e-12, atol=0)
+    assert np.array_equal(g, gr), f"max diff {np.abs(g - gr).max()} of {np.abs(gr).max()}"
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_gradient_vs_reference_fp64(name):
+    c = load(name)
+    a = c.args()
+    J, g = gb().misfit_and_gradient(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt, c["dobs"],
+                                    a["sponge"], a["src_list"], footprints=a["footprints"])
+    assert g.dtype == np.float64 and g.shape == c["m0"].shape
+    assert abs(J - float(c["J"])) <= 1e-4 * abs(float(c["J"]))
+    assert rel_l2(g, c["g"]) < grad_tol(name)
+
+
+@pytest.mark.parametrize("name", ["ring2d_point", "cyl3d_aperture", "parity3d", "ring2d_sponge"])
+def test_checkpoint_recompute_bit_exact(name):
+    """k = nt-1: one segment, the stash is filled by the forward sweep itself
+    (no recompute); smaller k recompute every earlier segment from stored
+    levels -- the gradients must agree bit for bit."""
+    c = load(name)
+    a = c.args()
+    res = []
+    for k in (c.nt - 1, 2, 3, 16):
+        _, g = gb().misfit_and_gradient(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt,
+                                        c["dobs"], a["sponge"], a["src_list"],
+                                        footprints=a["footprints"], batch=2, ckpt_k=k)
+        res.append(g)
+    for g in res[1:]:
+        assert np.array_equal(g, res[0])
+
+
+@pytest.mark.parametrize("name", ["parity2d", "gpu3d"])
+def test_batched_equals_one_shot_per_launch(name):
+    c = load(name)
+    a = c.args()
+    m = torch.from_numpy(c["m_true"]).cuda()
+    ds = [gb().forward_fmc(m, c.geom, a["wavelet"], c.dt, c.h, c.nt, None, a["src_list"],
+                           batch=C).cpu().numpy() for C in (1, 4, 16)]
+    assert np.array_equal(ds[0], ds[1]) and np.array_equal(ds[0], ds[2])
+
+
+def test_gauss_newton_hessian_vector():
+    c = load("gn2d")
+    hv32, born32 = oracle.gn_hessian_vector32(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["v"],
+                                              src_list=c.src_list, C=2)
+    hv, born = gb().gn_hessian_vector(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["v"],
+                                      src_list=c.src_list, batch=2, ckpt_k=7, return_born=True)
+    assert np.array_equal(born.astype(np.float32), born32)
+    assert np.array_equal(hv, hv32)
+    assert rel_l2(hv, c["Hv"]) < 1e-4
+
+
+def test_gauss_newton_3d_vs_fp64_oracle():
+    c = load("parity3d")
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal(c["m0"].shape)
+    v[:3] = v[-3:] = v[:, :3] = v[:, -3:] = v[:, :, :3] = v[:, :, -3:] = 0.0
+    v *= float(np.mean(c["m0"])) * 0.01
+    sl = c.src_list[:3]
+    ref = oracle.gn_hessian_vector(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, v, src_list=sl)
+    hv = gb().gn_hessian_vector(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, v, src_list=sl)
+    assert rel_l2(hv, ref) < 1e-4
+
+
+@pytest.mark.parametrize("name", ["parity2d", "gpu3d", "odd3d"])
+def test_plain_one_shot_form(name):
+    c = load(name)
+    d = gb().plain_forward_fmc(c["m_true"], c.geom, c.wavelet, c.dt, c.h, c.nt, c.src_list)
+    assert rel_l2(d, c["dobs"]) < trace_tol(name)
+    J, g = gb().plain_misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                                          c.src_list)
+    assert abs(J - float(c["J"])) <= 1e-4 * abs(float(c["J"]))
+    assert rel_l2(g, c["g"]) < grad_tol(name)
+
+
+def test_host_pointer_abi_matches_reference_core():
+    """usct_forward_fmc / usct_misfit_and_gradient take the arguments of
+    uap::forward_fmc / uap::misfit_and_gradient (libuap.hpp:109,169)."""
+    from openusct_gb300 import _lib
+    from openusct_gb300.geometry import linear_indices
+    lib = _lib.load()
+    c = load("parity3d")
+    m = np.ascontiguousarray(c["m_true"])
+    dims = (ctypes.c_int * 3)(*m.shape)
+    rec = linear_indices(c.geom.idx, m.shape).astype(np.int32)
+    tx = np.ascontiguousarray(rec[c.src_list])
+    data = np.zeros((len(tx), c.nt, len(rec)))
+    _lib.check(lib.usct_forward_fmc(m.ctypes.data_as(_lib._dp), dims, 3, c.h, c.dt, c.nt,
+                                    tx.ctypes.data_as(_lib._ip), len(tx),
+                                    rec.ctypes.data_as(_lib._ip), len(rec),
+                                    c.wavelet.ctypes.data_as(_lib._dp),
+                                    data.ctypes.data_as(_lib._dp)))
+    assert rel_l2(data, c["dobs_cpp"]) < 1e-5
+    g = np.zeros(m.shape)
+    J = ctypes.c_double()
+    m0 = np.ascontiguousarray(c["m0"])
+    dobs = np.ascontiguousarray(c["dobs"])
+    _lib.check(lib.usct_misfit_and_gradient(m0.ctypes.data_as(_lib._dp), dims, 3, c.h, c.dt, c.nt,
+                                            tx.ctypes.data_as(_lib._ip), len(tx),
+                                            rec.ctypes.data_as(_lib._ip), len(rec),
+                                            c.wavelet.ctypes.data_as(_lib._dp),
+                                            dobs.ctypes.data_as(_lib._dp),
+                                            g.ctypes.data_as(_lib._dp), ctypes.byref(J)))
+    assert abs(J.value - float(c["J_cpp"])) <= 1e-4 * float(c["J_cpp"])
+    assert rel_l2(g, c["g_cpp"]) < 1e-4
+
+
+def test_directional_derivatives_eight_seeded_directions():
+    """GPU gradient . dm against a central difference of the FP64 misfit along
+    8 seeded directions (the reference's test_gradient_misfits.py pattern)."""
+    c = load("parity3d")
+    sl = c.src_list[:3]
+    m0 = c["m0"]
+    _, g = gb().misfit_and_gradient(m0, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"][:3],
+                                    src_list=sl)
+    rng = np.random.default_rng(1)
+    for _ in range(8):
+        dm = rng.standard_normal(m0.shape)
+        dm[:3] = dm[-3:] = dm[:, :3] = dm[:, -3:] = dm[:, :, :3] = dm[:, :, -3:] = 0.0
+        dm *= float(np.mean(m0))
+        eps = 1e-6
+        Jp = oracle.misfit(m0 + eps * dm, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"][:3],
+                           src_list=sl)
+        Jm = oracle.misfit(m0 - eps * dm, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"][:3],
+                           src_list=sl)
+        fd = (Jp - Jm) / (2 * eps)
+        assert abs(float(np.sum(g * dm)) - fd) <= 1e-4 * abs(fd)
+
+
+def test_error_conventions():
+    c = load("ring2d_point")
+    with pytest.raises(NotImplementedError):
+        gb().misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                                 src_list=c.src_list, misfit_type="gcn")
+    with pytest.raises(ValueError):
+        gb().misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                                 src_list=c.src_list, misfit_type="nope")
+    with pytest.raises(ValueError):
+        gb().misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"][:1],
+                                 src_list=c.src_list)
