@@ -172,7 +172,8 @@ def _setup(m, geom, h, dt, nt, src_list, footprints, mode, batch, ckpt_k, tile):
     if not batch:
         free, _total = torch.cuda.mem_get_info()
         budget = int(0.7 * free)
-        batch = choose_batch(shape, nt, rx.rows, len(rx.cell), ckpt_k or 0, mode, budget)
+        batch = choose_batch(shape, nt, tx.rows, rx.rows, len(rx.cell), ckpt_k or 0, mode,
+                             budget)
     tile = tile or (0, 0, 0)
     return get_plan(shape, h, dt, nt, tx, rx, batch, ckpt_k or 0, *tile)
 
