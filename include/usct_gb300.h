@@ -196,6 +196,31 @@ int usct_misfit_and_gradient(const double* m, const int* dims, int ndim, double 
                              int nt, const int* tx_lin, int n_tx, const int* rec_lin, int n_rec,
                              const double* wavelet, const double* dobs, double* grad, double* J);
 
+/* ---- a forward FMC that allocates no device memory ---- */
+/*
+ * No counterpart in the reference.  For callers that may not allocate device
+ * memory -- a host that has reserved the GPU for its own pool allocator, a
+ * plugin inside such a host, a real-time loop that must not enter the CUDA
+ * allocator.  Same result as usct_forward_fmc_dev (point or footprint
+ * elements, optional sponge), but it needs no plan and no workspace: all
+ * scratch lives in one static device array of USCT_NOALLOC_SCRATCH_BYTES that
+ * every GPU loading the library holds until exit; larger problems are
+ * rejected with USCT_ERR_ARG.  It calls no cudaMalloc/cudaFree.
+ *   dims/h/dt/nt and the CSR arrays: as usct_plan_create (host arrays)
+ *   m, sponge (NULL = none), wavelet: device FP64; data: device FP32
+ *   [n_tx][nt][n_rx], caller-allocated.
+ * The first call on a device resolves the array's device address (with that
+ * device current); make it before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race on it and must be serialised.
+ */
+#define USCT_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+int usct_forward_fmc_noalloc(int ndim, const int* dims, double h, double dt, int nt,
+                             int n_tx, const int* tx_ptr, const int64_t* tx_cell,
+                             const double* tx_w, int n_rx, const int* rx_ptr,
+                             const int64_t* rx_cell, const double* rx_w, const double* m,
+                             const double* sponge, const double* wavelet, float* data,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif

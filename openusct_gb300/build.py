@@ -1,6 +1,6 @@
 """Build recipe for the CUDA library ``openusct_gb300/libusct_gb300.so``.
 
-One translation unit, one ``-gencode`` (sm_103a), built in-tree with nvcc.
+Two translation units, one ``-gencode`` (sm_103a), built in-tree with nvcc.
 ``-fmad=false`` keeps every multiply-add unfused unless the kernels ask for
 ``__fmaf_rn`` explicitly, which fixes the rounding of the stencil so the CPU
 restatement can reproduce it bit for bit.
@@ -16,8 +16,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "libusct_gb300.so")
-SOURCES = ["usct_engine.cu"]
-DEPS = ["usct_engine.cu", "usct_kernels.cuh", "usct_plain.cuh"]
+SOURCES = ["usct_engine.cu", "usct_noalloc.cu"]
+DEPS = ["usct_engine.cu", "usct_noalloc.cu", "usct_kernels.cuh", "usct_plain.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

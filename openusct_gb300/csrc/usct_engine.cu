@@ -57,6 +57,12 @@ static int set_err(int code, const char* fmt, ...) {
     } while (0)
 
 extern "C" const char* usct_last_error(void) { return g_err.c_str(); }
+
+// Error reporting for the other translation units of the library.
+int usct_internal_error(int code, const char* msg) {
+    g_err = msg ? msg : "";
+    return code;
+}
 extern "C" int usct_version(void) { return 10000; }
 
 // ---------------------------------------------------------------------------
