@@ -65,6 +65,11 @@ extern "C" {
 #define USCT_INFO_ZCHUNK 6       /* planes marched per CTA */
 #define USCT_INFO_LEVEL_FLOATS 7 /* floats in one batched wavefield level */
 #define USCT_INFO_LAUNCHES 8     /* kernels launched by this plan so far */
+#define USCT_INFO_VARIANT 9      /* 0 = register-queue stencils, 1 = TMA ring */
+
+/* usct_plan_set keys */
+#define USCT_SET_VARIANT 0       /* 0 = register-queue stencils, 1 = TMA-fed ring */
+#define USCT_SET_STAGES 1        /* planes in the TMA ring (3..8) */
 
 /* One-line message describing the last error on this thread ("" if none). */
 const char* usct_last_error(void);
@@ -95,6 +100,12 @@ int usct_plan_create(usct_plan** out, int ndim, const int* dims, double h, doubl
                      int batch, int ckpt_k, int tile_x, int tile_y, int zchunk);
 void usct_plan_destroy(usct_plan* plan);
 int usct_plan_info(const usct_plan* plan, int key, int64_t* value);
+/* Tuning knobs (USCT_SET_*): the stencil variant and the TMA ring depth.  The
+ * default is the TMA ring wherever its box constraints hold. */
+int usct_plan_set(usct_plan* plan, int key, int64_t value);
+/* Synchronise the stream and report a pipelined stencil that gave up waiting
+ * for its tensor copies (bounded waits; USCT_ERR_CUDA), then clear the flag. */
+int usct_plan_check(usct_plan* plan, void* stream);
 
 /* Bytes of the model workspace (S, sponge, v/m, wavelet, FP64 gradient). */
 size_t usct_model_bytes(const usct_plan* plan);

@@ -26,7 +26,8 @@ MODE_GRADIENT = 1
 MODE_BORN = 2
 
 INFO = {"batch": 0, "nbatch": 1, "ckpt_k": 2, "nseg": 3, "tile_x": 4, "tile_y": 5,
-        "zchunk": 6, "level_floats": 7, "launches": 8}
+        "zchunk": 6, "level_floats": 7, "launches": 8, "variant": 9}
+SET = {"variant": 0, "stages": 1}
 
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
@@ -43,6 +44,8 @@ SIGNATURES = {
                               _lp, _dp, _i, _i, _i, _i, _i]),
     "usct_plan_destroy": (None, [_vp]),
     "usct_plan_info": (_i, [_vp, _i, _lp]),
+    "usct_plan_set": (_i, [_vp, _i, ctypes.c_int64]),
+    "usct_plan_check": (_i, [_vp, _vp]),
     "usct_model_bytes": (ctypes.c_size_t, [_vp]),
     "usct_batch_bytes": (ctypes.c_size_t, [_vp, _i]),
     "usct_model_prepare": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),

@@ -60,7 +60,7 @@ class Plan:
     """A ``usct_plan``: grid, time axis, elements and batching on one device."""
 
     def __init__(self, shape, h, dt, nt, tx: CSR, rx: CSR, batch=0, ckpt_k=0, tile_x=0,
-                 tile_y=0, zchunk=0):
+                 tile_y=0, zchunk=0, variant=None, stages=None):
         _require_cuda()
         lib = _lib.load()
         self.shape = tuple(int(s) for s in shape)
@@ -78,6 +78,17 @@ class Plan:
             int(ckpt_k), int(tile_x), int(tile_y), int(zchunk)))
         self._p = ptr
         self._lib = lib
+        if variant is not None:
+            self.set("variant", int(variant))
+        if stages is not None:
+            self.set("stages", int(stages))
+
+    def set(self, key, value):
+        _lib.check(self._lib.usct_plan_set(self._p, _lib.SET[key], int(value)))
+
+    def check(self, stream=None):
+        """Synchronise and raise if a pipelined kernel gave up waiting."""
+        _lib.check(self._lib.usct_plan_check(self._p, _stream(stream)))
 
     @property
     def handle(self):
@@ -149,12 +160,14 @@ _PLANS: "OrderedDict[tuple, Plan]" = OrderedDict()
 _MAX_PLANS = 8
 
 
-def get_plan(shape, h, dt, nt, tx, rx, batch=0, ckpt_k=0, tile_x=0, tile_y=0, zchunk=0):
+def get_plan(shape, h, dt, nt, tx, rx, batch=0, ckpt_k=0, tile_x=0, tile_y=0, zchunk=0,
+             variant=None, stages=None):
     key = (tuple(shape), float(h), float(dt), int(nt), tx.key(), rx.key(), int(batch),
-           int(ckpt_k), int(tile_x), int(tile_y), int(zchunk), torch.cuda.current_device())
+           int(ckpt_k), int(tile_x), int(tile_y), int(zchunk), variant, stages,
+           torch.cuda.current_device())
     p = _PLANS.get(key)
     if p is None:
-        p = Plan(shape, h, dt, nt, tx, rx, batch, ckpt_k, tile_x, tile_y, zchunk)
+        p = Plan(shape, h, dt, nt, tx, rx, batch, ckpt_k, tile_x, tile_y, zchunk, variant, stages)
         _PLANS[key] = p
         while len(_PLANS) > _MAX_PLANS:
             _PLANS.popitem(last=False)[1].close()
@@ -174,7 +187,12 @@ def _setup(m, geom, h, dt, nt, src_list, footprints, mode, batch, ckpt_k, tile):
         budget = int(0.7 * free)
         batch = choose_batch(shape, nt, tx.rows, rx.rows, len(rx.cell), ckpt_k or 0, mode,
                              budget)
-    tile = tile or (0, 0, 0)
+    tile = tuple(tile) if tile else ()
+    if len(tile) < 3:
+        from .autotune import lookup
+        tuned = lookup(shape, batch)
+        tile = tuple(tuned) if tuned else (0, 0, 0)
+    tile = tile + (None,) * (5 - len(tile))
     return get_plan(shape, h, dt, nt, tx, rx, batch, ckpt_k or 0, *tile)
 
 
@@ -214,6 +232,7 @@ def forward_fmc(m, geom, wavelet, dt, h, nt, sponge=None, src_list=None, footpri
     bws = _workspace(plan.batch_bytes(_lib.MODE_FORWARD), dev)
     _lib.check(plan._lib.usct_forward_fmc_dev(plan.handle, _ptr(md), _ptr(sd), _ptr(wd),
                                               _ptr(data), _ptr(mws), _ptr(bws), _stream()))
+    plan.check()
     return _out(data, m)
 
 
@@ -239,6 +258,7 @@ def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list
     _lib.check(plan._lib.usct_misfit_and_gradient_dev(
         plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(od), _ptr(J), _ptr(g), _ptr(mws),
         _ptr(bws), _stream()))
+    plan.check()
     Jh = J.cpu().numpy()
     Jv = float(np.sum(Jh))
     if return_per_shot:
@@ -267,6 +287,7 @@ def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, misfit
         _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
                                           _lib.MODE_FORWARD, None, s))
         _lib.check(lib.usct_batch_misfit(plan.handle, _ptr(bws), b, _ptr(od), _ptr(J), s))
+    plan.check()
     return float(np.sum(J.cpu().numpy()))
 
 
@@ -293,6 +314,7 @@ def gn_hessian_vector(m, geom, wavelet, dt, h, nt, v, sponge=None, src_list=None
     _lib.check(plan._lib.usct_gn_hessian_vector_dev(
         plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(vd), _ptr(hv), _ptr(born), _ptr(mws),
         _ptr(bws), _stream()))
+    plan.check()
     if return_born:
         return _out(hv, m), _out(born, m)
     return _out(hv, m)

@@ -17,7 +17,7 @@ REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "libusct_gb300.so")
 SOURCES = ["usct_engine.cu", "usct_noalloc.cu"]
-DEPS = ["usct_engine.cu", "usct_noalloc.cu", "usct_kernels.cuh", "usct_plain.cuh"]
+DEPS = ["usct_engine.cu", "usct_noalloc.cu", "usct_kernels.cuh", "usct_plain.cuh", "usct_tma.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

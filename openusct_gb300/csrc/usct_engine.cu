@@ -13,17 +13,21 @@
 // Memory per batch (levels of nz*ny*nxs*C floats): 2 state + 2*nseg
 // checkpoints + k stash + 2 adjoint (+2 Born), see usct_batch_bytes.
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "usct_gb300.h"
 #include "usct_kernels.cuh"
+#include "usct_tma.cuh"
 
 using namespace usct;
 
@@ -93,6 +97,11 @@ struct usct_plan {
     int64_t* d_rx_cell = nullptr;
     bool has_sp = false, has_vm = false;
     long long launches = 0;
+    // kernel variant: 0 = register-queue stencils, 1 = TMA-fed shared-memory ring
+    int variant = 0;
+    int stages_fwd = 5, stages_born = 4, stages_adj = 4;
+    int* d_err = nullptr;   // set by a kernel whose bounded wait gave up
+    std::unordered_map<uint64_t, CUtensorMap> maps;
 };
 
 static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -104,9 +113,20 @@ static bool tile_supported(bool is3d, int txv, int ty) {
     return ty == 1 && (txv == 64 || txv == 128);
 }
 
+// The TMA ring needs 16-byte rows in every box: a tile row must hold at least
+// 4 cells of the model (TXF >= 4C), and for batches narrower than 4 shots
+// (boxes of whole rows) the row box must fit 256 elements (tile_x == 32, 3D).
+static bool tma_supported(const usct_plan* p) {
+    const int TXF = 4 * p->txv;
+    if (p->C >= 4) return (TXF >> p->logC) % 4 == 0;
+    return p->ndim == 3 && p->txv == 32;
+}
+
 static void free_plan_dev(usct_plan* p) {
     cudaFree(p->d_sptr); cudaFree(p->d_sent); cudaFree(p->d_rptr); cudaFree(p->d_rent);
     cudaFree(p->d_rxptr); cudaFree(p->d_tx_cell); cudaFree(p->d_tx_w); cudaFree(p->d_rx_cell);
+    cudaFree(p->d_err);
+    p->d_err = nullptr;
     p->d_sptr = nullptr; p->d_sent = nullptr; p->d_rptr = nullptr; p->d_rent = nullptr;
     p->d_rxptr = nullptr; p->d_tx_cell = nullptr; p->d_tx_w = nullptr; p->d_rx_cell = nullptr;
 }
@@ -296,11 +316,13 @@ extern "C" int usct_plan_create(usct_plan** out, int ndim, const int* dims, doub
         (ret = upload(&p->d_rxptr, rxptr)) != USCT_OK ||
         (ret = upload(&p->d_tx_cell, p->h_tx_cell)) != USCT_OK ||
         (ret = upload(&p->d_tx_w, txwf)) != USCT_OK ||
-        (ret = upload(&p->d_rx_cell, p->h_rx_cell)) != USCT_OK) {
+        (ret = upload(&p->d_rx_cell, p->h_rx_cell)) != USCT_OK ||
+        (ret = upload(&p->d_err, std::vector<int>(1, 0))) != USCT_OK) {
         free_plan_dev(p);
         delete p;
         return ret;
     }
+    p->variant = tma_supported(p) ? 1 : 0;
     *out = p;
     return USCT_OK;
 }
@@ -323,6 +345,7 @@ extern "C" int usct_plan_info(const usct_plan* p, int key, int64_t* value) {
         case USCT_INFO_ZCHUNK: *value = p->geo.zc; break;
         case USCT_INFO_LEVEL_FLOATS: *value = (int64_t)p->LV; break;
         case USCT_INFO_LAUNCHES: *value = p->launches; break;
+        case USCT_INFO_VARIANT: *value = p->variant; break;
         default: return set_err(USCT_ERR_ARG, "unknown info key %d", key);
     }
     return USCT_OK;
@@ -505,8 +528,182 @@ static size_t stencil_smem(const usct_plan* p, int nfield) {
     return sizeof(float) * 2 * nfield * (p->ty + 2) * (4 * p->txv + 2 * HF);
 }
 
+// ---- tensor maps for the TMA ring -------------------------------------------
+enum MapKind { MK_WF_HALO = 0, MK_WF_OWN = 1, MK_CELL_OWN = 2, MK_CELL_HALO = 3, MK_G_OWN = 4 };
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+    });
+    return fn;
+}
+
+// Box shapes (innermost first).  Wavefields: 4D {C, nxs, ny, nz} when C >= 4,
+// otherwise 3D {RP, ny, nz}; model cells: 3D {nxs, ny, nz} (float or double).
+static int get_map(usct_plan* p, const void* ptr, int kind, CUtensorMap* out) {
+    const uint64_t key = (uint64_t)(uintptr_t)ptr * 8u + (uint64_t)kind;
+    auto it = p->maps.find(key);
+    if (it != p->maps.end()) { *out = it->second; return USCT_OK; }
+    auto enc = encode_fn();
+    if (!enc) return set_err(USCT_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    const Geo& g = p->geo;
+    const int TXF = 4 * p->txv, cells = TXF >> g.logC, HR = p->ndim == 3 ? 1 : 0;
+    const int rows_h = p->ty + 2 * HR;
+    cuuint64_t dims[4] = {0, 0, 0, 0}, strides[3] = {0, 0, 0};
+    cuuint32_t box[4] = {1, 1, 1, 1}, estr[4] = {1, 1, 1, 1};
+    cuuint32_t rank = 3;
+    CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const bool halo = kind == MK_WF_HALO;
+    if (kind == MK_WF_HALO || kind == MK_WF_OWN) {
+        if (g.C >= 4) {
+            rank = 4;
+            dims[0] = g.C; dims[1] = g.nxs; dims[2] = g.ny; dims[3] = g.nz;
+            strides[0] = (cuuint64_t)g.C * 4; strides[1] = (cuuint64_t)g.RP * 4;
+            strides[2] = (cuuint64_t)g.PP * 4;
+            box[0] = g.C; box[1] = cells + (halo ? 2 : 0); box[2] = halo ? rows_h : p->ty; box[3] = 1;
+        } else {
+            dims[0] = g.RP; dims[1] = g.ny; dims[2] = g.nz;
+            strides[0] = (cuuint64_t)g.RP * 4; strides[1] = (cuuint64_t)g.PP * 4;
+            box[0] = TXF + (halo ? 8 : 0); box[1] = halo ? rows_h : p->ty; box[2] = 1;
+        }
+    } else {
+        const int es = kind == MK_G_OWN ? 8 : 4;
+        if (kind == MK_G_OWN) dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+        dims[0] = g.nxs; dims[1] = g.ny; dims[2] = g.nz;
+        strides[0] = (cuuint64_t)g.nxs * es; strides[1] = (cuuint64_t)g.CPP * es;
+        box[0] = cells + (kind == MK_CELL_HALO ? 8 : 0);
+        box[1] = kind == MK_CELL_HALO ? rows_h : p->ty;
+        box[2] = 1;
+    }
+    for (cuuint32_t d = 0; d < rank; ++d)
+        if (box[d] > 256 || box[d] == 0) return set_err(USCT_ERR_ARG, "TMA box dim %u = %u", d, box[d]);
+    if ((uintptr_t)ptr % 16 != 0) return set_err(USCT_ERR_ARG, "TMA base address not 16-byte aligned");
+    CUtensorMap m;
+    CUresult r = enc(&m, dt, rank, const_cast<void*>(ptr), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_err(USCT_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    if (p->maps.size() > 4096) p->maps.clear();
+    p->maps.emplace(key, m);
+    *out = m;
+    return USCT_OK;
+}
+
+static int smem_optin() {
+    static int v = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    });
+    return v;
+}
+
+template <class K>
+static int prepare_smem(K kernel, size_t smem) {
+    if (smem > (size_t)smem_optin()) return set_err(USCT_ERR_ARG, "TMA ring needs %zu B of shared memory", smem);
+    if (smem > 48 * 1024) CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return USCT_OK;
+}
+
+#define USCT_FWD_TMA_CASE(TX, TY_, D3)                                                        \
+    case TX * 1000 + TY_: {                                                                  \
+        auto k = k_forward_tma<TX, TY_, D3, BORN>;                                           \
+        TRY(prepare_smem(k, smem));                                                          \
+        k<<<grid, dim3(TX, TY_), smem, s>>>(a, mp, R, p->d_err);                             \
+    } break;
+
+template <bool BORN>
+static int launch_fwd_tma(usct_plan* p, const FwdArgs& a, cudaStream_t s) {
+    FwdMaps mp;
+    memset(&mp, 0, sizeof(mp));
+    TRY(get_map(p, a.pc, MK_WF_HALO, &mp.pc));
+    TRY(get_map(p, a.pp, MK_WF_OWN, &mp.pp));
+    TRY(get_map(p, a.S, MK_CELL_OWN, &mp.S));
+    if (a.sp) TRY(get_map(p, a.sp, MK_CELL_OWN, &mp.sp));
+    if (BORN) {
+        TRY(get_map(p, a.dc, MK_WF_HALO, &mp.dc));
+        TRY(get_map(p, a.dpp, MK_WF_OWN, &mp.dpp));
+        TRY(get_map(p, a.vm, MK_CELL_OWN, &mp.vm));
+    }
+    const int R = BORN ? p->stages_born : p->stages_fwd;
+    const FwdStage L = fwd_stage(p->txv, p->ty, p->ndim == 3, BORN, p->C, p->logC, a.sp != nullptr);
+    const size_t smem = (size_t)R * L.floats * sizeof(float) + (size_t)R * 8 + 16;
+    const dim3 grid(p->ntx_t, p->nty_t, p->nzc);
+    const int key = p->txv * 1000 + p->ty;
+    if (p->ndim == 3) {
+        switch (key) {
+            USCT_FWD_TMA_CASE(32, 4, true)
+            USCT_FWD_TMA_CASE(32, 8, true)
+            USCT_FWD_TMA_CASE(64, 2, true)
+            USCT_FWD_TMA_CASE(64, 4, true)
+            default: return set_err(USCT_ERR_ARG, "no 3D TMA kernel for tile %d", key);
+        }
+    } else {
+        switch (key) {
+            USCT_FWD_TMA_CASE(64, 1, false)
+            USCT_FWD_TMA_CASE(128, 1, false)
+            default: return set_err(USCT_ERR_ARG, "no 2D TMA kernel for tile %d", key);
+        }
+    }
+    ++p->launches;
+    CUDA_TRY(cudaGetLastError());
+    return USCT_OK;
+}
+
+#define USCT_ADJ_TMA_CASE(TX, TY_, D3)                                                        \
+    case TX * 1000 + TY_: {                                                                  \
+        auto k = k_adjoint_tma<TX, TY_, D3>;                                                 \
+        TRY(prepare_smem(k, smem));                                                          \
+        k<<<grid, dim3(TX, TY_), smem, s>>>(a, mp, R, p->d_err);                             \
+    } break;
+
+static int launch_adj_tma(usct_plan* p, const AdjArgs& a, cudaStream_t s) {
+    AdjMaps mp;
+    memset(&mp, 0, sizeof(mp));
+    TRY(get_map(p, a.l1, MK_WF_HALO, &mp.l1));
+    TRY(get_map(p, a.S, MK_CELL_HALO, &mp.S));
+    TRY(get_map(p, a.l2, MK_WF_OWN, &mp.l2));
+    TRY(get_map(p, a.d2, MK_WF_OWN, &mp.d2));
+    if (a.sp) TRY(get_map(p, a.sp, MK_CELL_OWN, &mp.sp));
+    if (a.gacc) TRY(get_map(p, a.gacc, MK_G_OWN, &mp.g));
+    const int R = p->stages_adj;
+    const AdjStage L = adj_stage(p->txv, p->ty, p->ndim == 3, p->C, p->logC, a.sp != nullptr,
+                                 a.gacc != nullptr);
+    const size_t smem = (size_t)R * L.floats * sizeof(float) + (size_t)R * 8 + 16;
+    const dim3 grid(p->ntx_t, p->nty_t, p->nzc);
+    const int key = p->txv * 1000 + p->ty;
+    if (p->ndim == 3) {
+        switch (key) {
+            USCT_ADJ_TMA_CASE(32, 4, true)
+            USCT_ADJ_TMA_CASE(32, 8, true)
+            USCT_ADJ_TMA_CASE(64, 2, true)
+            USCT_ADJ_TMA_CASE(64, 4, true)
+            default: return set_err(USCT_ERR_ARG, "no 3D TMA kernel for tile %d", key);
+        }
+    } else {
+        switch (key) {
+            USCT_ADJ_TMA_CASE(64, 1, false)
+            USCT_ADJ_TMA_CASE(128, 1, false)
+            default: return set_err(USCT_ERR_ARG, "no 2D TMA kernel for tile %d", key);
+        }
+    }
+    ++p->launches;
+    CUDA_TRY(cudaGetLastError());
+    return USCT_OK;
+}
+
 template <bool BORN>
 static int launch_fwd(usct_plan* p, const FwdArgs& a, cudaStream_t s) {
+    if (p->variant == 1) return launch_fwd_tma<BORN>(p, a, s);
     const dim3 grid(p->ntx_t, p->nty_t, p->nzc);
     const size_t smem = stencil_smem(p, BORN ? 2 : 1);
     const int key = p->txv * 1000 + p->ty;
@@ -531,6 +728,7 @@ static int launch_fwd(usct_plan* p, const FwdArgs& a, cudaStream_t s) {
 }
 
 static int launch_adj(usct_plan* p, const AdjArgs& a, cudaStream_t s) {
+    if (p->variant == 1) return launch_adj_tma(p, a, s);
     const dim3 grid(p->ntx_t, p->nty_t, p->nzc);
     const size_t smem = stencil_smem(p, 1);
     const int key = p->txv * 1000 + p->ty;
@@ -551,6 +749,37 @@ static int launch_adj(usct_plan* p, const AdjArgs& a, cudaStream_t s) {
     }
     ++p->launches;
     CUDA_TRY(cudaGetLastError());
+    return USCT_OK;
+}
+
+extern "C" int usct_plan_set(usct_plan* p, int key, int64_t value) {
+    if (!p) return set_err(USCT_ERR_ARG, "null plan");
+    switch (key) {
+        case USCT_SET_VARIANT:
+            if (value != 0 && value != 1) return set_err(USCT_ERR_ARG, "variant must be 0 or 1");
+            if (value == 1 && !tma_supported(p))
+                return set_err(USCT_ERR_ARG, "the TMA variant needs tile_x*4 >= 4*batch (or tile_x = 32 in 3D)");
+            p->variant = (int)value;
+            return USCT_OK;
+        case USCT_SET_STAGES:
+            if (value < 3 || value > 8) return set_err(USCT_ERR_ARG, "stages must be 3..8");
+            p->stages_fwd = (int)value;
+            p->stages_born = (int)std::max<int64_t>(3, value - 1);
+            p->stages_adj = (int)std::max<int64_t>(3, value - 1);
+            return USCT_OK;
+        default: return set_err(USCT_ERR_ARG, "unknown setting %d", key);
+    }
+}
+
+extern "C" int usct_plan_check(usct_plan* p, void* stream) {
+    if (!p) return set_err(USCT_ERR_ARG, "null plan");
+    CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    int flag = 0;
+    CUDA_TRY(cudaMemcpy(&flag, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+        CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
+        return set_err(USCT_ERR_CUDA, "a pipelined stencil gave up waiting for its tensor copies");
+    }
     return USCT_OK;
 }
 

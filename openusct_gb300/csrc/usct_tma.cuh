@@ -1,0 +1,591 @@
+// usct_tma.cuh -- TMA-fed pipelined variants of the forward and adjoint stencils.
+//
+// Same arithmetic, same op order, same outputs as k_forward / k_adjoint
+// (usct_kernels.cuh); only the way planes reach shared memory differs.  Each
+// CTA keeps a ring of R plane stages in shared memory.  One elected thread
+// issues cp.async.bulk.tensor copies (one per field per plane: the halo tile
+// of p^{n-1} -- TY+2 rows of (cells+2)*C floats --, the own tile of p^{n-2},
+// the model cells) for plane z+R-1 while every warp computes plane z from the
+// stages of z-1, z and z+1; completion is tracked by one mbarrier per stage
+// (expect_tx byte counts).  Bytes in flight per SM no longer cost registers,
+// which is what limited the register-queue kernels (long-scoreboard stalls at
+// 25 % occupancy).  Out-of-range planes, rows and cells are zero-filled by the
+// tensor copy itself.
+//
+// Waits are bounded: a stage that does not complete within kWaitNs sets *err,
+// the CTA drains (again bounded) the copies it issued and returns; once *err is
+// set every later launch returns before issuing anything, and the host reports
+// the flag (usct_plan_check).
+#pragma once
+
+#include <cuda.h>
+
+#include "usct_kernels.cuh"
+
+namespace usct {
+
+constexpr unsigned long long kWaitNs = 250000000ull;   // 250 ms per stage wait
+constexpr int kSpinCap = 1 << 26;                      // backstop on the poll count
+
+struct FwdMaps {
+    CUtensorMap pc, pp, S, sp, dc, dpp, vm;
+};
+struct AdjMaps {
+    CUtensorMap l1, S, l2, d2, sp, g;
+};
+
+__host__ __device__ constexpr int al32(int x) { return (x + 31) & ~31; }
+
+// Stage layout in floats, shared by host (smem sizing) and device.
+struct FwdStage {
+    int o_pp, o_S, o_sp, o_dc, o_dpp, o_vm, floats;
+};
+__host__ __device__ inline FwdStage fwd_stage(int TXV, int TY, bool is3d, bool born, int C, int logC,
+                                              bool has_sp) {
+    const int HF = C < 4 ? 4 : C;
+    const int TXF = 4 * TXV;
+    const int rows = TY + (is3d ? 2 : 0);
+    const int SR = TXF + 2 * HF;
+    const int cells = TXF >> logC;
+    FwdStage s{};
+    s.o_pp = al32(rows * SR);
+    s.o_S = s.o_pp + al32(TY * TXF);
+    s.o_sp = s.o_S + al32(TY * cells);
+    int end = s.o_sp + (has_sp ? al32(TY * cells) : 0);
+    s.o_dc = end;
+    if (born) {
+        s.o_dpp = s.o_dc + al32(rows * SR);
+        s.o_vm = s.o_dpp + al32(TY * TXF);
+        end = s.o_vm + al32(TY * cells);
+    }
+    s.floats = end;
+    return s;
+}
+
+struct AdjStage {
+    int o_S, o_l2, o_d2, o_sp, o_g, floats;
+};
+__host__ __device__ inline AdjStage adj_stage(int TXV, int TY, bool is3d, int C, int logC, bool has_sp,
+                                              bool has_g) {
+    const int HF = C < 4 ? 4 : C;
+    const int TXF = 4 * TXV;
+    const int rows = TY + (is3d ? 2 : 0);
+    const int SR = TXF + 2 * HF;
+    const int cells = TXF >> logC;
+    AdjStage s{};
+    s.o_S = al32(rows * SR);
+    s.o_l2 = s.o_S + al32(rows * (cells + 8));
+    s.o_d2 = s.o_l2 + al32(TY * TXF);
+    s.o_sp = s.o_d2 + al32(TY * TXF);
+    s.o_g = s.o_sp + (has_sp ? al32(TY * cells) : 0);
+    s.floats = s.o_g + (has_g ? al32(2 * TY * cells) : 0);
+    return s;
+}
+
+// ---- PTX wrappers ----------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// bounded wait for local plane i of a ring of R stages
+__device__ __forceinline__ bool wait_stage(uint64_t* bars, int i, int R) {
+    uint64_t* b = bars + (i % R);
+    const uint32_t parity = (uint32_t)((i / R) & 1);
+    if (mbar_try_wait(b, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (int it = 1; it < kSpinCap; ++it) {
+        if (mbar_try_wait(b, parity)) return true;
+        if ((it & 255) == 0 && global_ns() - t0 > kWaitNs) return false;
+    }
+    return false;
+}
+// every thread of the CTA learns whether an earlier wait already gave up
+// (flag word in shared memory right after the R stage barriers)
+__device__ __forceinline__ bool aborted(const int* err, int* s_abort) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) *s_abort = *reinterpret_cast<const volatile int*>(err);
+    __syncthreads();
+    return *s_abort != 0;
+}
+__device__ __forceinline__ void tma3(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
+                                     int c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2)
+        : "memory");
+}
+__device__ __forceinline__ void tma4(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
+                                     int c2, int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%3, %4, %5, %6}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2),
+        "r"(c3)
+        : "memory");
+}
+
+// cell-layout row (smem) expanded to the 4 floats starting at float lf
+__device__ __forceinline__ float4 cell4s(const float* row, int lf, int logC) {
+    if (logC == 0) return ld4(row + lf);
+    if (logC == 1) {
+        const float2 s = *reinterpret_cast<const float2*>(row + (lf >> 1));
+        return make_float4(s.x, s.x, s.y, s.y);
+    }
+    const float s = row[lf >> logC];
+    return make_float4(s, s, s, s);
+}
+
+__device__ __forceinline__ float4 mul4(const float4& a, const float4& b) {
+    return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w);
+}
+
+// ---------------------------------------------------------------------------
+// forward step, TMA ring
+// ---------------------------------------------------------------------------
+template <int TXV, int TY, bool IS3D, bool BORN>
+__global__ void __launch_bounds__(TXV* TY) k_forward_tma(const FwdArgs a, const __grid_constant__ FwdMaps mp,
+                                                         const int R, int* err) {
+    extern __shared__ __align__(128) float smf[];
+    const Geo& g = a.g;
+    const int C = g.C, logC = g.logC;
+    const int HF = C < 4 ? 4 : C;
+    constexpr int HR = IS3D ? 1 : 0;
+    constexpr int TXF = 4 * TXV;
+    constexpr int ROWS = TY + 2 * HR;
+    const int SR = TXF + 2 * HF;
+    const int cells = TXF >> logC;
+    const bool has_sp = a.sp != nullptr;
+    const FwdStage L = fwd_stage(TXV, TY, IS3D, BORN, C, logC, has_sp);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smf + (size_t)R * L.floats);
+
+    const int tx = threadIdx.x;
+    const int ty = (TY > 1) ? (int)threadIdx.y : 0;
+    const int tid = tx + TXV * ty;
+    const int fx0 = blockIdx.x * TXF;
+    const int x0c = fx0 >> logC;
+    const int y0 = blockIdx.y * TY;
+    const int z0 = blockIdx.z * g.zc;
+    const int z1 = min(z0 + g.zc, g.nz);
+    const int nloc = z1 - z0 + 2;   // local planes z0-1 .. z1
+    const int f = fx0 + 4 * tx;
+    const int y = y0 + ty;
+    const bool own = (f < g.RP) && (y < g.ny);
+    const int col = HF + 4 * tx;
+    const int r = ty + HR;
+    const long long ro = (long long)y * g.RP + f;
+    const bool y_in = !IS3D || (y >= 1 && y <= g.ny - 2);
+    bool x_in[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int xq = (f + q) >> logC;
+        x_in[q] = xq >= 1 && xq <= g.nx - 2;
+    }
+    const float cen = IS3D ? -6.f : -4.f;
+    const float inv_h2 = g.inv_h2;
+    const float wv = a.wav[a.n - 1];
+
+    const uint32_t b_halo = (uint32_t)(ROWS * SR * 4), b_own = (uint32_t)(TY * TXF * 4),
+                   b_cell = (uint32_t)(TY * cells * 4);
+    auto issue = [&](int i) {
+        const int p = z0 - 1 + i;
+        const int slot = i % R;
+        float* st = smf + (size_t)slot * L.floats;
+        uint64_t* bar = bars + slot;
+        const bool inner = i >= 1 && i <= nloc - 2;
+        uint32_t bytes = b_halo * (BORN ? 2u : 1u);
+        if (inner) bytes += b_own * (BORN ? 2u : 1u) + b_cell * (1u + (has_sp ? 1u : 0u) + (BORN ? 1u : 0u));
+        mbar_expect_tx(bar, bytes);
+        if (C >= 4) tma4(st, &mp.pc, bar, 0, x0c - 1, y0 - HR, p);
+        else tma3(st, &mp.pc, bar, fx0 - 4, y0 - HR, p);
+        if (BORN) {
+            if (C >= 4) tma4(st + L.o_dc, &mp.dc, bar, 0, x0c - 1, y0 - HR, p);
+            else tma3(st + L.o_dc, &mp.dc, bar, fx0 - 4, y0 - HR, p);
+        }
+        if (inner) {
+            if (C >= 4) tma4(st + L.o_pp, &mp.pp, bar, 0, x0c, y0, p);
+            else tma3(st + L.o_pp, &mp.pp, bar, fx0, y0, p);
+            tma3(st + L.o_S, &mp.S, bar, x0c, y0, p);
+            if (has_sp) tma3(st + L.o_sp, &mp.sp, bar, x0c, y0, p);
+            if (BORN) {
+                if (C >= 4) tma4(st + L.o_dpp, &mp.dpp, bar, 0, x0c, y0, p);
+                else tma3(st + L.o_dpp, &mp.dpp, bar, fx0, y0, p);
+                tma3(st + L.o_vm, &mp.vm, bar, x0c, y0, p);
+            }
+        }
+    };
+
+    if (aborted(err, reinterpret_cast<int*>(bars + R))) return;
+    if (tid == 0) {
+        for (int s = 0; s < R; ++s) mbar_init(bars + s, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const int npro = min(R, nloc);
+    if (tid == 0)
+        for (int i = 0; i < npro; ++i) issue(i);
+    int issued = npro;
+
+    // per-tile entry cursors
+    const int tile = blockIdx.x + g.ntiles_x * blockIdx.y;
+    int si = a.s_ptr ? a.s_ptr[tile] : 0;
+    const int se = a.s_ptr ? a.s_ptr[tile + 1] : 0;
+    while (si < se && a.s_ent[si].z < z0) ++si;
+    int snz = si < se ? a.s_ent[si].z : 0x7fffffff;
+    int ri = 0, re = 0;
+    if (a.rs) {
+        ri = a.r_ptr[tile];
+        re = a.r_ptr[tile + 1];
+        while (ri < re && a.r_ent[ri].z < z0) ++ri;
+    }
+    int rnz = ri < re ? a.r_ent[ri].z : 0x7fffffff;
+
+    bool ok = wait_stage(bars, 0, R);
+    ok = wait_stage(bars, 1, R) && ok;
+    for (int z = z0; z < z1; ++z) {
+        const int im = z - z0;
+        ok = wait_stage(bars, im + 2, R) && ok;
+        const float* sm_m = smf + (size_t)(im % R) * L.floats;
+        const float* sm_c = smf + (size_t)((im + 1) % R) * L.floats;
+        const float* sm_p = smf + (size_t)((im + 2) % R) * L.floats;
+
+        const float4 cc = ld4(sm_c + r * SR + col);
+        float4 xm, xp;
+        xnb(sm_c + r * SR, col, C, cc, xm, xp);
+        float4 ym = f4zero(), yp = f4zero();
+        if (IS3D) {
+            ym = ld4(sm_c + (r - 1) * SR + col);
+            yp = ld4(sm_c + (r + 1) * SR + col);
+        }
+        const float4 cm = ld4(sm_m + r * SR + col);
+        const float4 cp = ld4(sm_p + r * SR + col);
+        const float4 ppv = ld4(sm_c + L.o_pp + ty * TXF + 4 * tx);
+        const float4 Sv = cell4s(sm_c + L.o_S + ty * cells, 4 * tx, logC);
+        const float4 spv = has_sp ? cell4s(sm_c + L.o_sp + ty * cells, 4 * tx, logC) : f4zero();
+        const bool zy_in = y_in && z >= 1 && z <= g.nz - 2;
+        float lap[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            lap[q] = stencil(zy_in && x_in[q], cen, comp(cc, q), comp(xm, q), comp(xp, q),
+                             comp(ym, q), comp(yp, q), comp(cm, q), comp(cp, q), IS3D, inv_h2);
+        if (z == snz) {
+            while (si < se) {
+                const SrcEnt e = a.s_ent[si];
+                if (e.z != z) break;
+                if (e.ly == ty) {
+                    const int d = e.f - 4 * tx;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        if (d == q) lap[q] = lap[q] + e.w * wv;
+                }
+                ++si;
+            }
+            snz = si < se ? a.s_ent[si].z : 0x7fffffff;
+        }
+        float pn[4], d2v[4], out[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float c = comp(cc, q);
+            float v = __fmaf_rn(comp(Sv, q), lap[q], 2.f * c - comp(ppv, q));
+            if (has_sp) v = v * comp(spv, q);
+            d2v[q] = (v - 2.f * c) + comp(ppv, q);
+            pn[q] = v;
+            out[q] = v;
+        }
+        if (BORN) {
+            const float* dcs = sm_c + L.o_dc;
+            const float4 dcc = ld4(dcs + r * SR + col);
+            float4 dxm, dxp;
+            xnb(dcs + r * SR, col, C, dcc, dxm, dxp);
+            float4 dym = f4zero(), dyp = f4zero();
+            if (IS3D) {
+                dym = ld4(dcs + (r - 1) * SR + col);
+                dyp = ld4(dcs + (r + 1) * SR + col);
+            }
+            const float4 dm = ld4(sm_m + L.o_dc + r * SR + col);
+            const float4 dp = ld4(sm_p + L.o_dc + r * SR + col);
+            const float4 dppv = ld4(sm_c + L.o_dpp + ty * TXF + 4 * tx);
+            const float4 vmv = cell4s(sm_c + L.o_vm + ty * cells, 4 * tx, logC);
+            float dv[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float dl = stencil(zy_in && x_in[q], cen, comp(dcc, q), comp(dxm, q),
+                                         comp(dxp, q), comp(dym, q), comp(dyp, q), comp(dm, q),
+                                         comp(dp, q), IS3D, inv_h2);
+                float v = __fmaf_rn(comp(Sv, q), dl, 2.f * comp(dcc, q) - comp(dppv, q));
+                v = __fmaf_rn(-comp(vmv, q), d2v[q], v);
+                if (has_sp) v = v * comp(spv, q);
+                dv[q] = v;
+                out[q] = v;
+            }
+            if (own) st4(a.dn + z * g.PP + ro, make_float4(dv[0], dv[1], dv[2], dv[3]));
+        }
+        if (own) {
+            const float4 v = make_float4(pn[0], pn[1], pn[2], pn[3]);
+            st4(a.pn + z * g.PP + ro, v);
+            if (a.ck) st4(a.ck + z * g.PP + ro, v);
+            if (a.d2) st4(a.d2 + z * g.PP + ro, make_float4(d2v[0], d2v[1], d2v[2], d2v[3]));
+        }
+        if (z == rnz) {
+            while (ri < re) {
+                const RxEnt e = a.r_ent[ri];
+                if (e.z != z) break;
+                if (e.ly == ty) {
+                    const int base = e.lcell * C - 4 * tx;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int c = q - base;
+                        if (c >= 0 && c < C) a.rs[(long long)e.slot * C + c] = e.w * out[q];
+                    }
+                }
+                ++ri;
+            }
+            rnz = ri < re ? a.r_ent[ri].z : 0x7fffffff;
+        }
+
+        // everyone is done with the stage of plane z-1: refill it with plane z-1+R
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) break;
+        if (tid == 0 && im + R < nloc) {
+            fence_proxy_async();
+            issue(im + R);
+        }
+        if (im + R < nloc) issued = im + R + 1;
+    }
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+        // drain what was issued so no copy lands in a retired CTA's memory
+        for (int i = (issued > R ? issued - R : 0); i < issued; ++i) (void)wait_stage(bars, i, R);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// adjoint step, TMA ring
+// ---------------------------------------------------------------------------
+template <int TXV, int TY, bool IS3D>
+__global__ void __launch_bounds__(TXV* TY) k_adjoint_tma(const AdjArgs a, const __grid_constant__ AdjMaps mp,
+                                                         const int R, int* err) {
+    extern __shared__ __align__(128) float smf[];
+    const Geo& g = a.g;
+    const int C = g.C, logC = g.logC;
+    const int HF = C < 4 ? 4 : C;
+    constexpr int HR = IS3D ? 1 : 0;
+    constexpr int TXF = 4 * TXV;
+    constexpr int ROWS = TY + 2 * HR;
+    const int SR = TXF + 2 * HF;
+    const int cells = TXF >> logC;
+    const int SH = cells + 8;   // S halo row length (cells)
+    const bool has_sp = a.sp != nullptr;
+    const bool has_g = a.gacc != nullptr;
+    const AdjStage L = adj_stage(TXV, TY, IS3D, C, logC, has_sp, has_g);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smf + (size_t)R * L.floats);
+
+    const int tx = threadIdx.x;
+    const int ty = (TY > 1) ? (int)threadIdx.y : 0;
+    const int tid = tx + TXV * ty;
+    const int fx0 = blockIdx.x * TXF;
+    const int x0c = fx0 >> logC;
+    const int y0 = blockIdx.y * TY;
+    const int z0 = blockIdx.z * g.zc;
+    const int z1 = min(z0 + g.zc, g.nz);
+    const int nloc = z1 - z0 + 2;
+    const int f = fx0 + 4 * tx;
+    const int y = y0 + ty;
+    const bool own = (f < g.RP) && (y < g.ny);
+    const int r = ty + HR;
+    const long long ro = (long long)y * g.RP + f;
+    const bool y_in = !IS3D || (y >= 1 && y <= g.ny - 2);
+    bool x_in[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int xq = (f + q) >> logC;
+        x_in[q] = xq >= 1 && xq <= g.nx - 2;
+    }
+    const float cen = IS3D ? -6.f : -4.f;
+    const float inv_h2 = g.inv_h2;
+
+    const uint32_t b_halo = (uint32_t)(ROWS * SR * 4), b_sh = (uint32_t)(ROWS * SH * 4),
+                   b_own = (uint32_t)(TY * TXF * 4), b_cell = (uint32_t)(TY * cells * 4);
+    auto issue = [&](int i) {
+        const int p = z0 - 1 + i;
+        const int slot = i % R;
+        float* st = smf + (size_t)slot * L.floats;
+        uint64_t* bar = bars + slot;
+        const bool inner = i >= 1 && i <= nloc - 2;
+        uint32_t bytes = b_halo + b_sh;
+        if (inner) bytes += 2 * b_own + (has_sp ? b_cell : 0u) + (has_g ? 2 * b_cell : 0u);
+        mbar_expect_tx(bar, bytes);
+        if (C >= 4) tma4(st, &mp.l1, bar, 0, x0c - 1, y0 - HR, p);
+        else tma3(st, &mp.l1, bar, fx0 - 4, y0 - HR, p);
+        tma3(st + L.o_S, &mp.S, bar, x0c - 4, y0 - HR, p);
+        if (inner) {
+            if (C >= 4) {
+                tma4(st + L.o_l2, &mp.l2, bar, 0, x0c, y0, p);
+                tma4(st + L.o_d2, &mp.d2, bar, 0, x0c, y0, p);
+            } else {
+                tma3(st + L.o_l2, &mp.l2, bar, fx0, y0, p);
+                tma3(st + L.o_d2, &mp.d2, bar, fx0, y0, p);
+            }
+            if (has_sp) tma3(st + L.o_sp, &mp.sp, bar, x0c, y0, p);
+            if (has_g) tma3(st + L.o_g, &mp.g, bar, x0c, y0, p);
+        }
+    };
+
+    if (aborted(err, reinterpret_cast<int*>(bars + R))) return;
+    if (tid == 0) {
+        for (int s = 0; s < R; ++s) mbar_init(bars + s, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const int npro = min(R, nloc);
+    if (tid == 0)
+        for (int i = 0; i < npro; ++i) issue(i);
+    int issued = npro;
+
+    const int tile = blockIdx.x + g.ntiles_x * blockIdx.y;
+    int ri = a.r_ptr[tile];
+    const int re = a.r_ptr[tile + 1];
+    while (ri < re && a.r_ent[ri].z < z0) ++ri;
+    int rnz = ri < re ? a.r_ent[ri].z : 0x7fffffff;
+
+    // q = S * lam^{k+1} at float lf (multiple of 4) / scalar, of a stage row
+    auto qv4 = [&](const float* st, int row, int lf) -> float4 {
+        const float4 l = ld4(st + row * SR + HF + lf);
+        const float4 s = cell4s(st + L.o_S + row * SH + 4, lf, logC);
+        return mul4(s, l);
+    };
+    auto qs = [&](const float* st, int row, int lf) -> float {
+        return st[L.o_S + row * SH + 4 + (lf >> logC)] * st[row * SR + HF + lf];
+    };
+
+    bool ok = wait_stage(bars, 0, R);
+    ok = wait_stage(bars, 1, R) && ok;
+    for (int z = z0; z < z1; ++z) {
+        const int im = z - z0;
+        ok = wait_stage(bars, im + 2, R) && ok;
+        const float* sm_m = smf + (size_t)(im % R) * L.floats;
+        const float* sm_c = smf + (size_t)((im + 1) % R) * L.floats;
+        const float* sm_p = smf + (size_t)((im + 2) % R) * L.floats;
+        const int lf = 4 * tx;
+        const float4 qc = qv4(sm_c, r, lf);
+        float4 xm, xp;
+        if (C >= 4) {
+            xm = qv4(sm_c, r, lf - C);
+            xp = qv4(sm_c, r, lf + C);
+        } else if (C == 2) {
+            xm = make_float4(qs(sm_c, r, lf - 2), qs(sm_c, r, lf - 1), qc.x, qc.y);
+            xp = make_float4(qc.z, qc.w, qs(sm_c, r, lf + 4), qs(sm_c, r, lf + 5));
+        } else {
+            xm = make_float4(qs(sm_c, r, lf - 1), qc.x, qc.y, qc.z);
+            xp = make_float4(qc.y, qc.z, qc.w, qs(sm_c, r, lf + 4));
+        }
+        float4 ym = f4zero(), yp = f4zero();
+        if (IS3D) {
+            ym = qv4(sm_c, r - 1, lf);
+            yp = qv4(sm_c, r + 1, lf);
+        }
+        const float4 qm = qv4(sm_m, r, lf);
+        const float4 qp = qv4(sm_p, r, lf);
+        const float4 l1c = ld4(sm_c + r * SR + HF + lf);
+        const float4 l2v = ld4(sm_c + L.o_l2 + ty * TXF + lf);
+        const float4 d2v = ld4(sm_c + L.o_d2 + ty * TXF + lf);
+        const float4 spv = has_sp ? cell4s(sm_c + L.o_sp + ty * cells, lf, logC) : f4zero();
+        const bool zy_in = y_in && z >= 1 && z <= g.nz - 2;
+        float lk[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float lq = stencil(zy_in && x_in[q], cen, comp(qc, q), comp(xm, q), comp(xp, q),
+                                     comp(ym, q), comp(yp, q), comp(qm, q), comp(qp, q), IS3D,
+                                     inv_h2);
+            float v = (2.f * comp(l1c, q) - comp(l2v, q)) + lq;
+            if (has_sp) v = v * comp(spv, q);
+            lk[q] = v;
+        }
+        if (z == rnz) {
+            while (ri < re) {
+                const RxEnt e = a.r_ent[ri];
+                if (e.z != z) break;
+                if (e.ly == ty) {
+                    const int base = e.lcell * C - 4 * tx;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int c = q - base;
+                        if (c >= 0 && c < C) lk[q] = lk[q] - a.res[(long long)e.j * C + c] * e.w;
+                    }
+                }
+                ++ri;
+            }
+            rnz = ri < re ? a.r_ent[ri].z : 0x7fffffff;
+        }
+        if (own) st4(a.lk + z * g.PP + ro, make_float4(lk[0], lk[1], lk[2], lk[3]));
+        if (has_g) {
+            float pr[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) pr[q] = own ? lk[q] * comp(d2v, q) : 0.f;
+            const double* gs = reinterpret_cast<const double*>(sm_c + L.o_g) + ty * cells;
+            double* grow = a.gacc + z * g.CPP + (long long)y * g.nxs + x0c;
+            if (logC == 0) {
+                if (own) {
+                    const int c0 = lf;
+                    double2* gp = reinterpret_cast<double2*>(grow + c0);
+                    gp[0] = make_double2(gs[c0] + (double)pr[0], gs[c0 + 1] + (double)pr[1]);
+                    gp[1] = make_double2(gs[c0 + 2] + (double)pr[2], gs[c0 + 3] + (double)pr[3]);
+                }
+            } else if (logC == 1) {
+                if (own) {
+                    const int c0 = lf >> 1;
+                    *reinterpret_cast<double2*>(grow + c0) =
+                        make_double2(gs[c0] + (double)(pr[0] + pr[1]), gs[c0 + 1] + (double)(pr[2] + pr[3]));
+                }
+            } else {
+                float s = (pr[0] + pr[1]) + (pr[2] + pr[3]);
+                const int G = C >> 2;
+                for (int o = 1; o < G; o <<= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
+                const int c0 = lf >> logC;
+                if (own && (tx & (G - 1)) == 0) grow[c0] = gs[c0] + (double)s;
+            }
+        }
+
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) break;
+        if (tid == 0 && im + R < nloc) {
+            fence_proxy_async();
+            issue(im + R);
+        }
+        if (im + R < nloc) issued = im + R + 1;
+    }
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+        for (int i = (issued > R ? issued - R : 0); i < issued; ++i) (void)wait_stage(bars, i, R);
+    }
+}
+
+}  // namespace usct

@@ -37,8 +37,13 @@ def gb():
 
 
 def _tiles(ndim):
-    return [(32, 4, 0), (32, 8, 3), (64, 2, 5), (64, 4, 0)] if ndim == 3 else [(64, 1, 0),
-                                                                               (128, 1, 7)]
+    """(tile_x, tile_y, zchunk, variant): variant 1 = TMA ring, 0 = register queue; the
+    TMA ring needs 4*tile_x >= 4*C (the plan reports an error otherwise, so such
+    combinations are skipped)."""
+    if ndim == 3:
+        return [(32, 4, 0, 1), (32, 8, 3, 1), (64, 2, 5, 1), (64, 4, 0, 1), (32, 8, 3, 0),
+                (64, 4, 0, 0)]
+    return [(64, 1, 0, 1), (128, 1, 7, 1), (64, 1, 0, 0), (128, 1, 7, 0)]
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -48,7 +53,9 @@ def test_forward_bit_exact_vs_fp32_restatement(name, C):
     a = c.args()
     ref = oracle.forward_fmc32(c["m_true"], c.geom, a["wavelet"], c.dt, c.h, c.nt, a["sponge"],
                                a["src_list"], a["footprints"])
-    for tile in _tiles(c["m_true"].ndim)[: 1 if C != 2 else None]:
+    for tile in _tiles(c["m_true"].ndim):
+        if tile[3] == 1 and C < 4 and (c["m_true"].ndim == 2 or tile[0] != 32):
+            continue   # outside the TMA ring's box constraints
         d = gb().forward_fmc(torch.from_numpy(c["m_true"]).cuda(), c.geom, a["wavelet"], c.dt,
                              c.h, c.nt, a["sponge"], a["src_list"], a["footprints"], batch=C,
                              tile=tile)
@@ -68,17 +75,22 @@ def test_forward_vs_reference_fp64(name):
 
 
 @pytest.mark.parametrize("name", CASES)
-@pytest.mark.parametrize("C", [1, 4])
-def test_gradient_bit_exact_vs_fp32_restatement(name, C):
+@pytest.mark.parametrize("C", [1, 4, 16])
+@pytest.mark.parametrize("variant", [0, 1])
+def test_gradient_bit_exact_vs_fp32_restatement(name, C, variant):
     c = load(name)
     a = c.args()
+    ndim = c["m0"].ndim
+    if variant == 1 and C < 4 and ndim == 2:
+        pytest.skip("the TMA ring needs C >= 4 in 2D")
+    tile = (32, 8, 0, variant) if ndim == 3 else (128, 1, 0, variant)
     Jr, gr = oracle.misfit_and_gradient32(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt,
                                           c["dobs"], a["sponge"], a["src_list"], a["footprints"],
                                           C=C)
     J, g, Js = gb().misfit_and_gradient(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt,
                                         c["dobs"], a["sponge"], a["src_list"],
                                         footprints=a["footprints"], batch=C, ckpt_k=5,
-                                        return_per_shot=True)
+                                        tile=tile, return_per_shot=True)
     assert np.allclose(Js, Jr, rtol=1e-12, atol=0)
     assert np.array_equal(g, gr), f"max diff {np.abs(g - gr).max()} of {np.abs(gr).max()}"
 
@@ -121,15 +133,32 @@ def test_batched_equals_one_shot_per_launch(name):
     assert np.array_equal(ds[0], ds[1]) and np.array_equal(ds[0], ds[2])
 
 
-def test_gauss_newton_hessian_vector():
+@pytest.mark.parametrize("C,variant", [(2, 0), (4, 1)])
+def test_gauss_newton_hessian_vector(C, variant):
     c = load("gn2d")
     hv32, born32 = oracle.gn_hessian_vector32(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["v"],
-                                              src_list=c.src_list, C=2)
+                                              src_list=c.src_list, C=C)
     hv, born = gb().gn_hessian_vector(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["v"],
-                                      src_list=c.src_list, batch=2, ckpt_k=7, return_born=True)
+                                      src_list=c.src_list, batch=C, ckpt_k=7,
+                                      tile=(128, 1, 0, variant), return_born=True)
     assert np.array_equal(born.astype(np.float32), born32)
     assert np.array_equal(hv, hv32)
     assert rel_l2(hv, c["Hv"]) < 1e-4
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+def test_gauss_newton_3d_bit_exact(variant):
+    c = load("gpu3d")
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal(c["m0"].shape) * float(np.mean(c["m0"])) * 0.01
+    sl = c.src_list[:4]
+    hv32, born32 = oracle.gn_hessian_vector32(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, v,
+                                              src_list=sl, C=4)
+    hv, born = gb().gn_hessian_vector(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, v,
+                                      src_list=sl, batch=4, ckpt_k=9,
+                                      tile=(32, 8, 0, variant), return_born=True)
+    assert np.array_equal(born.astype(np.float32), born32)
+    assert np.array_equal(hv, hv32)
 
 
 def test_gauss_newton_3d_vs_fp64_oracle():
