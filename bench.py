@@ -113,6 +113,59 @@ def cpu_gradient_sample(prob, shot, nt_sample, k):
                                   f"gradient (checkpoint k={k}), scaled by (nt-1)/{nt_sample - 1}")
 
 
+SERVE_STREAM = ("seeded Poisson stream at 20 req/s, 30% gradient / 70% forward, half 2D rings "
+                "(128^2-512^2, 32-128 elements) half 3D cylinders (64^3-128^3, 64-128 elements), "
+                "disc or random-field models, nt = 2.2*2R/1450/dt; HBM budget 150 GB, 6 slots")
+
+
+def serve_phase(args):
+    """Continuous-batching service on a scaled request stream: p50/p99 latency
+    and shots/s, against the same requests solved one shot at a time by the
+    plain one-shot-per-launch GPU form (timed on one shot of each request)."""
+    import numpy as np
+    import torch
+    import openusct_gb300.backend as gb
+    from openusct_gb300.serve import Engine, GpuExecutor, make_stream, summarize
+
+    def dobs_fn(m, geom, wav, dt, h, nt):
+        return gb.forward_fmc(m, geom, wav, dt, h, nt)
+
+    reqs = make_stream(args.serve_requests, rate_hz=20.0, seed=11, sizes_2d=(128, 512),
+                       sizes_3d=(64, 128), elements_2d=(32, 128), elements_3d=(64, 128),
+                       frac_gradient=0.3, dobs_fn=dobs_fn)
+    gb.release()
+    eng = Engine(GpuExecutor(), budget_bytes=150 << 30, max_active=6)
+    res = eng.run_stream(reqs)
+    st = summarize(res, eng)
+    # plain form: one shot of every request, timed with CUDA events, scaled by its shots
+    plain_s = 0.0
+    for q in reqs:
+        one = [0]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if q.kind == "forward":
+            gb.plain_forward_fmc(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt, src_list=one)
+            e0.record()
+            gb.plain_forward_fmc(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt, src_list=one)
+            e1.record()
+        else:
+            d1 = q.dobs[:1]
+            gb.plain_misfit_and_gradient(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt, d1, src_list=one)
+            e0.record()
+            gb.plain_misfit_and_gradient(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt, d1, src_list=one)
+            e1.record()
+        torch.cuda.synchronize()
+        plain_s += e0.elapsed_time(e1) / 1000.0 * q.n_shots
+    gb.release()
+    plain_rate = st.shots / plain_s if plain_s > 0 else None
+    return {"stream": SERVE_STREAM, "requests": st.n, "ok": st.ok, "rejected": st.rejected,
+            "p50_s": st.p50_s, "p99_s": st.p99_s, "mean_s": st.mean_s,
+            "makespan_s": st.makespan_s, "shots": st.shots, "shots_per_s": st.shots_per_s,
+            "max_concurrent": st.max_concurrent,
+            "peak_reserved_gb": st.peak_reserved_bytes / 2 ** 30,
+            "plain_sequential_shots_per_s": plain_rate,
+            "speedup_vs_plain_sequential": (st.shots_per_s / plain_rate) if plain_rate else None}
+
+
 def run_reference(args, prob):
     """--impl reference: the reference scheme's CPU path on the host cores."""
     import oracle
@@ -151,6 +204,8 @@ def main():
     ap.add_argument("--ckpt", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=24)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -295,6 +350,13 @@ def main():
                  "speedup_batched_vs_plain": value / world / (1.0 / tp)}
         del pws
 
+    serve = None
+    if rank == 0 and not args.no_serve:
+        try:
+            serve = serve_phase(args)
+        except Exception as exc:   # reported, never fatal for the main line
+            serve = {"error": f"{type(exc).__name__}: {exc}"[:300]}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -331,7 +393,7 @@ def main():
                                   "achieved": pipeline_bytes / (t_ms / 1000.0) / 1e9,
                                   "frac": pipeline_bytes / (t_ms / 1000.0) / 1e9 / hbm,
                                   "model": "44 B/shot + 20 B/batch per cell-step"},
-            "e2e": e2e, "plain": plain, "cpu_baseline": cpu,
+            "e2e": e2e, "plain": plain, "serve": serve, "cpu_baseline": cpu,
             "gpu_launches": launches, "clocks": clk.summary(),
         }
         print(json.dumps(line))

@@ -69,7 +69,10 @@ extern "C" {
 
 /* usct_plan_set keys */
 #define USCT_SET_VARIANT 0       /* 0 = register-queue stencils, 1 = TMA-fed ring */
-#define USCT_SET_STAGES 1        /* planes in the TMA ring (3..8) */
+#define USCT_SET_STAGES 1        /* planes in the forward TMA ring (3..8; Born uses one fewer) */
+#define USCT_SET_STAGES_ADJ 2    /* planes in the adjoint TMA ring (3..8) */
+#define USCT_SET_GRAPHS 3        /* 1 = capture each batch sweep as a CUDA graph on first
+                                    use (per stream/buffer set) and replay it afterwards */
 
 /* One-line message describing the last error on this thread ("" if none). */
 const char* usct_last_error(void);

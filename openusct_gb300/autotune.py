@@ -96,6 +96,8 @@ def time_kernels(shape, C, nt, tile, what=("fwd", "adj"), reps=2):
     plan = Plan(shape, h, dt, nt, tx, rx, batch=C, ckpt_k=max(2, nt - 1), tile_x=tile[0],
                 tile_y=tile[1], zchunk=tile[2], variant=tile[3] if len(tile) > 3 else None,
                 stages=tile[4] if len(tile) > 4 else None)
+    if len(tile) > 5:
+        plan.set("stages_adj", int(tile[5]))
     lib = _lib.load()
     dev = torch.device("cuda", torch.cuda.current_device())
     md = torch.from_numpy(m).to(dev)
@@ -139,7 +141,7 @@ def time_kernels(shape, C, nt, tile, what=("fwd", "adj"), reps=2):
         out["adj_GBs"] = (16 * C + 20) * cells / (out["adj_ms"] * 1e-3) / 1e9
     plan.check()
     out["tile"] = [plan.info("tile_x"), plan.info("tile_y"), plan.info("zchunk"),
-                   plan.info("variant")] + ([int(tile[4])] if len(tile) > 4 else [])
+                   plan.info("variant")] + [int(v) for v in tile[4:6]]
     plan.close()
     return out
 

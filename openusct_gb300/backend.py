@@ -42,6 +42,26 @@ def _stream(stream=None):
     return ctypes.c_void_p(s.cuda_stream)
 
 
+_EXEC_STREAMS = {}
+
+
+class _on_exec_stream:
+    """Run the engine on a private per-device stream (capturable, so batch
+    sweeps can be CUDA graphs) ordered after the caller's current stream."""
+
+    def __enter__(self):
+        dev = torch.cuda.current_device()
+        st = _EXEC_STREAMS.get(dev)
+        if st is None:
+            st = _EXEC_STREAMS[dev] = torch.cuda.Stream(device=dev)
+        st.wait_stream(torch.cuda.current_stream())
+        self.stream = st
+        return st
+
+    def __exit__(self, *exc):
+        torch.cuda.current_stream().wait_stream(self.stream)
+
+
 def _require_cuda():
     if not torch.cuda.is_available():
         raise RuntimeError("openusct_gb300 needs a CUDA device (there is no CPU fallback)")
@@ -82,6 +102,26 @@ class Plan:
             self.set("variant", int(variant))
         if stages is not None:
             self.set("stages", int(stages))
+        self._ws = {}
+        # launch-bound sizes replay whole batch sweeps as CUDA graphs
+        level = int(np.prod(self.shape)) * max(1, self.batch)
+        if level <= (1 << 22):
+            self.set("graphs", 1)
+
+    def workspace(self, kind, nbytes, device):
+        """A workspace kept with the plan (stable buffers let captured graphs
+        replay); very large ones are not kept."""
+        t = self._ws.get(kind)
+        if t is not None and t.numel() >= nbytes:
+            return t
+        t = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+        total = torch.cuda.get_device_properties(device).total_memory
+        if nbytes <= total // 8:
+            self._ws[kind] = t
+        return t
+
+    def release(self):
+        self._ws.clear()
 
     def set(self, key, value):
         _lib.check(self._lib.usct_plan_set(self._p, _lib.SET[key], int(value)))
@@ -117,6 +157,7 @@ class Plan:
         return int(self._lib.usct_plain_bytes(self._p, int(bool(gradient))))
 
     def close(self):
+        self._ws = {}
         if getattr(self, "_p", None) is not None and self._p.value:
             self._lib.usct_plan_destroy(self._p)
             self._p = ctypes.c_void_p()
@@ -227,12 +268,16 @@ def forward_fmc(m, geom, wavelet, dt, h, nt, sponge=None, src_list=None, footpri
     md = _to_dev(m, torch.float64, dev)
     wd = _to_dev(wavelet, torch.float64, dev)
     sd = _to_dev(sponge, torch.float64, dev)
-    data = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev)
-    mws = _workspace(plan.model_bytes(), dev)
-    bws = _workspace(plan.batch_bytes(_lib.MODE_FORWARD), dev)
-    _lib.check(plan._lib.usct_forward_fmc_dev(plan.handle, _ptr(md), _ptr(sd), _ptr(wd),
-                                              _ptr(data), _ptr(mws), _ptr(bws), _stream()))
-    plan.check()
+    nd = plan.n_tx * plan.nt * plan.n_rx
+    # a buffer kept with the plan, so a captured sweep replays into the same place
+    dbuf = plan.workspace("traces", 4 * nd, dev)[: 4 * nd].view(torch.float32)
+    mws = plan.workspace("model", plan.model_bytes(), dev)
+    bws = plan.workspace(_lib.MODE_FORWARD, plan.batch_bytes(_lib.MODE_FORWARD), dev)
+    with _on_exec_stream() as st:
+        _lib.check(plan._lib.usct_forward_fmc_dev(plan.handle, _ptr(md), _ptr(sd), _ptr(wd),
+                                                  _ptr(dbuf), _ptr(mws), _ptr(bws), _stream(st)))
+        plan.check(st)
+    data = dbuf.view(plan.n_tx, plan.nt, plan.n_rx).clone()
     return _out(data, m)
 
 
@@ -253,12 +298,13 @@ def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list
                          f"{(plan.n_tx, plan.nt, plan.n_rx)}")
     J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
     g = torch.empty(plan.shape, dtype=torch.float64, device=dev)
-    mws = _workspace(plan.model_bytes(), dev)
-    bws = _workspace(plan.batch_bytes(_lib.MODE_GRADIENT), dev)
-    _lib.check(plan._lib.usct_misfit_and_gradient_dev(
-        plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(od), _ptr(J), _ptr(g), _ptr(mws),
-        _ptr(bws), _stream()))
-    plan.check()
+    mws = plan.workspace("model", plan.model_bytes(), dev)
+    bws = plan.workspace(_lib.MODE_GRADIENT, plan.batch_bytes(_lib.MODE_GRADIENT), dev)
+    with _on_exec_stream() as st:
+        _lib.check(plan._lib.usct_misfit_and_gradient_dev(
+            plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(od), _ptr(J), _ptr(g), _ptr(mws),
+            _ptr(bws), _stream(st)))
+        plan.check(st)
     Jh = J.cpu().numpy()
     Jv = float(np.sum(Jh))
     if return_per_shot:
@@ -279,15 +325,18 @@ def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, misfit
     if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
         raise ValueError("dobs shape does not match the acquisition")
     J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
-    mws = _workspace(plan.model_bytes(), dev)
-    bws = _workspace(plan.batch_bytes(_lib.MODE_FORWARD), dev)
-    lib, s = plan._lib, _stream()
-    _lib.check(lib.usct_model_prepare(plan.handle, _ptr(mws), _ptr(md), _ptr(sd), None, _ptr(wd), s))
-    for b in range(plan.nbatch):
-        _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
-                                          _lib.MODE_FORWARD, None, s))
-        _lib.check(lib.usct_batch_misfit(plan.handle, _ptr(bws), b, _ptr(od), _ptr(J), s))
-    plan.check()
+    mws = plan.workspace("model", plan.model_bytes(), dev)
+    bws = plan.workspace(_lib.MODE_FORWARD, plan.batch_bytes(_lib.MODE_FORWARD), dev)
+    lib = plan._lib
+    with _on_exec_stream() as st:
+        s = _stream(st)
+        _lib.check(lib.usct_model_prepare(plan.handle, _ptr(mws), _ptr(md), _ptr(sd), None,
+                                          _ptr(wd), s))
+        for b in range(plan.nbatch):
+            _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
+                                              _lib.MODE_FORWARD, None, s))
+            _lib.check(lib.usct_batch_misfit(plan.handle, _ptr(bws), b, _ptr(od), _ptr(J), s))
+        plan.check(st)
     return float(np.sum(J.cpu().numpy()))
 
 
@@ -309,15 +358,23 @@ def gn_hessian_vector(m, geom, wavelet, dt, h, nt, v, sponge=None, src_list=None
     hv = torch.empty(plan.shape, dtype=torch.float64, device=dev)
     born = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev) \
         if return_born else None
-    mws = _workspace(plan.model_bytes(), dev)
-    bws = _workspace(plan.batch_bytes(_lib.MODE_BORN), dev)
-    _lib.check(plan._lib.usct_gn_hessian_vector_dev(
-        plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(vd), _ptr(hv), _ptr(born), _ptr(mws),
-        _ptr(bws), _stream()))
-    plan.check()
+    mws = plan.workspace("model", plan.model_bytes(), dev)
+    bws = plan.workspace(_lib.MODE_BORN, plan.batch_bytes(_lib.MODE_BORN), dev)
+    with _on_exec_stream() as st:
+        _lib.check(plan._lib.usct_gn_hessian_vector_dev(
+            plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(vd), _ptr(hv), _ptr(born), _ptr(mws),
+            _ptr(bws), _stream(st)))
+        plan.check(st)
     if return_born:
         return _out(hv, m), _out(born, m)
     return _out(hv, m)
+
+
+def release():
+    """Free every cached plan and workspace."""
+    while _PLANS:
+        _PLANS.popitem()[1].close()
+    torch.cuda.empty_cache()
 
 
 # ---------------------------------------------------------------------------

@@ -20,8 +20,11 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -99,10 +102,22 @@ struct usct_plan {
     long long launches = 0;
     // kernel variant: 0 = register-queue stencils, 1 = TMA-fed shared-memory ring
     int variant = 0;
-    int stages_fwd = 5, stages_born = 4, stages_adj = 4;
+    int stages_fwd = 4, stages_born = 3, stages_adj = 4;
     int* d_err = nullptr;   // set by a kernel whose bounded wait gave up
     std::unordered_map<uint64_t, CUtensorMap> maps;
+    // CUDA graphs of whole batch sweeps, keyed by (op, batch, mode, buffers)
+    bool use_graphs = false;
+    struct Captured {
+        cudaGraphExec_t exec;
+        long long kernels;
+    };
+    std::map<std::tuple<int, int, int, const void*, const void*, const void*>, Captured> graphs;
 };
+
+static void drop_graphs(usct_plan* p) {
+    for (auto& kv : p->graphs) cudaGraphExecDestroy(kv.second.exec);
+    p->graphs.clear();
+}
 
 static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 static int ilog2(int c) { int l = 0; while ((1 << l) < c) ++l; return l; }
@@ -116,6 +131,8 @@ static bool tile_supported(bool is3d, int txv, int ty) {
 // The TMA ring needs 16-byte rows in every box: a tile row must hold at least
 // 4 cells of the model (TXF >= 4C), and for batches narrower than 4 shots
 // (boxes of whole rows) the row box must fit 256 elements (tile_x == 32, 3D).
+static void init_tma_attributes();
+
 static bool tma_supported(const usct_plan* p) {
     const int TXF = 4 * p->txv;
     if (p->C >= 4) return (TXF >> p->logC) % 4 == 0;
@@ -323,12 +340,14 @@ extern "C" int usct_plan_create(usct_plan** out, int ndim, const int* dims, doub
         return ret;
     }
     p->variant = tma_supported(p) ? 1 : 0;
+    init_tma_attributes();
     *out = p;
     return USCT_OK;
 }
 
 extern "C" void usct_plan_destroy(usct_plan* p) {
     if (!p) return;
+    drop_graphs(p);
     free_plan_dev(p);
     delete p;
 }
@@ -609,9 +628,31 @@ static int smem_optin() {
 
 template <class K>
 static int prepare_smem(K kernel, size_t smem) {
+    (void)kernel;
     if (smem > (size_t)smem_optin()) return set_err(USCT_ERR_ARG, "TMA ring needs %zu B of shared memory", smem);
-    if (smem > 48 * 1024) CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return USCT_OK;
+}
+
+// Opt every TMA kernel into the device's full dynamic shared memory once, at
+// plan creation (outside any stream capture).
+template <class K>
+static void allow_smem(K kernel) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin());
+}
+static void init_tma_attributes() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        allow_smem(k_forward_tma<32, 4, true, false>);  allow_smem(k_forward_tma<32, 4, true, true>);
+        allow_smem(k_forward_tma<32, 8, true, false>);  allow_smem(k_forward_tma<32, 8, true, true>);
+        allow_smem(k_forward_tma<64, 2, true, false>);  allow_smem(k_forward_tma<64, 2, true, true>);
+        allow_smem(k_forward_tma<64, 4, true, false>);  allow_smem(k_forward_tma<64, 4, true, true>);
+        allow_smem(k_forward_tma<64, 1, false, false>); allow_smem(k_forward_tma<64, 1, false, true>);
+        allow_smem(k_forward_tma<128, 1, false, false>); allow_smem(k_forward_tma<128, 1, false, true>);
+        allow_smem(k_adjoint_tma<32, 4, true>);  allow_smem(k_adjoint_tma<32, 8, true>);
+        allow_smem(k_adjoint_tma<64, 2, true>);  allow_smem(k_adjoint_tma<64, 4, true>);
+        allow_smem(k_adjoint_tma<64, 1, false>); allow_smem(k_adjoint_tma<128, 1, false>);
+        cudaGetLastError();
+    });
 }
 
 #define USCT_FWD_TMA_CASE(TX, TY_, D3)                                                        \
@@ -765,7 +806,14 @@ extern "C" int usct_plan_set(usct_plan* p, int key, int64_t value) {
             if (value < 3 || value > 8) return set_err(USCT_ERR_ARG, "stages must be 3..8");
             p->stages_fwd = (int)value;
             p->stages_born = (int)std::max<int64_t>(3, value - 1);
-            p->stages_adj = (int)std::max<int64_t>(3, value - 1);
+            return USCT_OK;
+        case USCT_SET_STAGES_ADJ:
+            if (value < 3 || value > 8) return set_err(USCT_ERR_ARG, "stages must be 3..8");
+            p->stages_adj = (int)value;
+            return USCT_OK;
+        case USCT_SET_GRAPHS:
+            p->use_graphs = value != 0;
+            if (!p->use_graphs) drop_graphs(p);
             return USCT_OK;
         default: return set_err(USCT_ERR_ARG, "unknown setting %d", key);
     }
@@ -835,6 +883,46 @@ static int gather(usct_plan* p, const BatchWS& B, int b, float* out, const float
     return USCT_OK;
 }
 
+// Run `enqueue` directly, or -- with graphs on and a capturable stream -- as a
+// CUDA graph captured on first use for this (op, batch, mode, buffers) key and
+// replayed afterwards (the kernels read everything else from the buffers, so
+// a replay recomputes with the buffers' current contents).
+static int run_graph(usct_plan* p, cudaStream_t s, int op, int b, int mode, const void* k0,
+                     const void* k1, const void* k2, const std::function<int()>& enqueue) {
+    if (!p->use_graphs || s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread)
+        return enqueue();
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    CUDA_TRY(cudaStreamIsCapturing(s, &st));
+    if (st != cudaStreamCaptureStatusNone) return enqueue();   // the caller is capturing
+    const auto key = std::make_tuple(op, b, mode, k0, k1, k2);
+    auto it = p->graphs.find(key);
+    if (it == p->graphs.end()) {
+        if (p->graphs.size() >= 64) drop_graphs(p);
+        const long long before = p->launches;
+        CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue();
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(s, &graph);
+        if (rc != USCT_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        CUDA_TRY(e);
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CUDA_TRY(ei);
+        it = p->graphs.emplace(key, usct_plan::Captured{exec, p->launches - before}).first;
+        p->launches = before;
+    }
+    CUDA_TRY(cudaGraphLaunch(it->second.exec, s));
+    p->launches += it->second.kernels;
+    return USCT_OK;
+}
+
+static int batch_forward_impl(usct_plan* p, const void* model_ws, void* batch_ws, int b, int mode,
+                              float* traces, cudaStream_t s);
+
 extern "C" int usct_batch_forward(usct_plan* p, const void* model_ws, void* batch_ws, int b,
                                   int mode, float* traces, void* stream) {
     if (!p || !model_ws || !batch_ws) return set_err(USCT_ERR_ARG, "null argument");
@@ -843,6 +931,14 @@ extern "C" int usct_batch_forward(usct_plan* p, const void* model_ws, void* batc
     if (mode == USCT_MODE_BORN && !p->has_vm)
         return set_err(USCT_ERR_STATE, "Born sweep needs a model prepared with v");
     cudaStream_t s = (cudaStream_t)stream;
+    // the sponge choice is baked into captured launches: key on it too
+    const void* k2 = (const void*)((uintptr_t)traces ^ (p->has_sp ? (uintptr_t)1 : 0));
+    return run_graph(p, s, 1, b, mode, model_ws, batch_ws, k2,
+                     [&] { return batch_forward_impl(p, model_ws, batch_ws, b, mode, traces, s); });
+}
+
+static int batch_forward_impl(usct_plan* p, const void* model_ws, void* batch_ws, int b, int mode,
+                              float* traces, cudaStream_t s) {
     const ModelWS M = carve_model(p, (void*)model_ws);
     const BatchWS B = carve_batch(p, batch_ws, mode);
     const size_t lvb = al256(p->LV * sizeof(float));
@@ -917,10 +1013,18 @@ extern "C" int usct_batch_adjoint_source(usct_plan* p, void* batch_ws, int b, co
     return USCT_OK;
 }
 
+static int batch_backward_impl(usct_plan* p, void* model_ws, void* batch_ws, int b, cudaStream_t s);
+
 extern "C" int usct_batch_backward(usct_plan* p, void* model_ws, void* batch_ws, int b, void* stream) {
     if (!p || !model_ws || !batch_ws) return set_err(USCT_ERR_ARG, "null argument");
     if (b < 0 || b >= p->nbatch) return set_err(USCT_ERR_ARG, "batch %d out of range", b);
     cudaStream_t s = (cudaStream_t)stream;
+    const void* k2 = (const void*)(uintptr_t)(p->has_sp ? 1 : 0);
+    return run_graph(p, s, 2, b, 0, model_ws, batch_ws, k2,
+                     [&] { return batch_backward_impl(p, model_ws, batch_ws, b, s); });
+}
+
+static int batch_backward_impl(usct_plan* p, void* model_ws, void* batch_ws, int b, cudaStream_t s) {
     const ModelWS M = carve_model(p, model_ws);
     const BatchWS B = carve_batch(p, batch_ws, USCT_MODE_GRADIENT);
     const size_t lvb = al256(p->LV * sizeof(float));

@@ -116,10 +116,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
     asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
     return t;
 }
-// bounded wait for local plane i of a ring of R stages
-__device__ __forceinline__ bool wait_stage(uint64_t* bars, int i, int R) {
-    uint64_t* b = bars + (i % R);
-    const uint32_t parity = (uint32_t)((i / R) & 1);
+// bounded wait for the stage barrier b to complete the phase of the given parity
+__device__ __forceinline__ bool wait_bar(uint64_t* b, uint32_t parity) {
     if (mbar_try_wait(b, parity)) return true;
     const unsigned long long t0 = global_ns();
     for (int it = 1; it < kSpinCap; ++it) {
@@ -127,6 +125,10 @@ __device__ __forceinline__ bool wait_stage(uint64_t* bars, int i, int R) {
         if ((it & 255) == 0 && global_ns() - t0 > kWaitNs) return false;
     }
     return false;
+}
+// local plane i of a ring of R stages (used on the rare drain path only)
+__device__ __forceinline__ bool wait_stage(uint64_t* bars, int i, int R) {
+    return wait_bar(bars + (i % R), (uint32_t)((i / R) & 1));
 }
 // every thread of the CTA learns whether an earlier wait already gave up
 // (flag word in shared memory right after the R stage barriers)
@@ -215,9 +217,8 @@ __global__ void __launch_bounds__(TXV* TY) k_forward_tma(const FwdArgs a, const 
 
     const uint32_t b_halo = (uint32_t)(ROWS * SR * 4), b_own = (uint32_t)(TY * TXF * 4),
                    b_cell = (uint32_t)(TY * cells * 4);
-    auto issue = [&](int i) {
+    auto issue = [&](int i, int slot) {
         const int p = z0 - 1 + i;
-        const int slot = i % R;
         float* st = smf + (size_t)slot * L.floats;
         uint64_t* bar = bars + slot;
         const bool inner = i >= 1 && i <= nloc - 2;
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(TXV* TY) k_forward_tma(const FwdArgs a, const 
     __syncthreads();
     const int npro = min(R, nloc);
     if (tid == 0)
-        for (int i = 0; i < npro; ++i) issue(i);
+        for (int i = 0; i < npro; ++i) issue(i, i);
     int issued = npro;
 
     // per-tile entry cursors
@@ -268,14 +269,22 @@ __global__ void __launch_bounds__(TXV* TY) k_forward_tma(const FwdArgs a, const 
     }
     int rnz = ri < re ? a.r_ent[ri].z : 0x7fffffff;
 
-    bool ok = wait_stage(bars, 0, R);
-    ok = wait_stage(bars, 1, R) && ok;
+    // ring bookkeeping without divisions: slots of local planes im, im+1, im+2
+    // and the phase parity of the stage being waited for
+    int s_m = 0, s_c = 1, s_p = 2 % R;
+    uint32_t ph_p = (R == 2) ? 1u : 0u;
+    bool ok = wait_bar(bars + 0, 0u);
+    ok = wait_bar(bars + 1, 0u) && ok;
+    float* pn_ptr = a.pn + (long long)z0 * g.PP + ro;
+    float* ck_ptr = a.ck ? a.ck + (long long)z0 * g.PP + ro : nullptr;
+    float* d2_ptr = a.d2 ? a.d2 + (long long)z0 * g.PP + ro : nullptr;
+    float* dn_ptr = BORN ? a.dn + (long long)z0 * g.PP + ro : nullptr;
     for (int z = z0; z < z1; ++z) {
         const int im = z - z0;
-        ok = wait_stage(bars, im + 2, R) && ok;
-        const float* sm_m = smf + (size_t)(im % R) * L.floats;
-        const float* sm_c = smf + (size_t)((im + 1) % R) * L.floats;
-        const float* sm_p = smf + (size_t)((im + 2) % R) * L.floats;
+        ok = wait_bar(bars + s_p, ph_p) && ok;
+        const float* sm_m = smf + (size_t)s_m * L.floats;
+        const float* sm_c = smf + (size_t)s_c * L.floats;
+        const float* sm_p = smf + (size_t)s_p * L.floats;
 
         const float4 cc = ld4(sm_c + r * SR + col);
         float4 xm, xp;
@@ -346,14 +355,18 @@ __global__ void __launch_bounds__(TXV* TY) k_forward_tma(const FwdArgs a, const 
                 dv[q] = v;
                 out[q] = v;
             }
-            if (own) st4(a.dn + z * g.PP + ro, make_float4(dv[0], dv[1], dv[2], dv[3]));
+            if (own) st4(dn_ptr, make_float4(dv[0], dv[1], dv[2], dv[3]));
         }
         if (own) {
             const float4 v = make_float4(pn[0], pn[1], pn[2], pn[3]);
-            st4(a.pn + z * g.PP + ro, v);
-            if (a.ck) st4(a.ck + z * g.PP + ro, v);
-            if (a.d2) st4(a.d2 + z * g.PP + ro, make_float4(d2v[0], d2v[1], d2v[2], d2v[3]));
+            st4(pn_ptr, v);
+            if (ck_ptr) st4(ck_ptr, v);
+            if (d2_ptr) st4(d2_ptr, make_float4(d2v[0], d2v[1], d2v[2], d2v[3]));
         }
+        pn_ptr += g.PP;
+        if (ck_ptr) ck_ptr += g.PP;
+        if (d2_ptr) d2_ptr += g.PP;
+        if (BORN) dn_ptr += g.PP;
         if (z == rnz) {
             while (ri < re) {
                 const RxEnt e = a.r_ent[ri];
@@ -376,9 +389,12 @@ __global__ void __launch_bounds__(TXV* TY) k_forward_tma(const FwdArgs a, const 
         if (!ok) break;
         if (tid == 0 && im + R < nloc) {
             fence_proxy_async();
-            issue(im + R);
+            issue(im + R, s_m);
         }
         if (im + R < nloc) issued = im + R + 1;
+        s_m = s_c;
+        s_c = s_p;
+        if (++s_p == R) { s_p = 0; ph_p ^= 1u; }
     }
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);
@@ -391,7 +407,7 @@ __global__ void __launch_bounds__(TXV* TY) k_forward_tma(const FwdArgs a, const 
 // adjoint step, TMA ring
 // ---------------------------------------------------------------------------
 template <int TXV, int TY, bool IS3D>
-__global__ void __launch_bounds__(TXV* TY) k_adjoint_tma(const AdjArgs a, const __grid_constant__ AdjMaps mp,
+__global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_tma(const AdjArgs a, const __grid_constant__ AdjMaps mp,
                                                          const int R, int* err) {
     extern __shared__ __align__(128) float smf[];
     const Geo& g = a.g;
@@ -434,9 +450,8 @@ __global__ void __launch_bounds__(TXV* TY) k_adjoint_tma(const AdjArgs a, const 
 
     const uint32_t b_halo = (uint32_t)(ROWS * SR * 4), b_sh = (uint32_t)(ROWS * SH * 4),
                    b_own = (uint32_t)(TY * TXF * 4), b_cell = (uint32_t)(TY * cells * 4);
-    auto issue = [&](int i) {
+    auto issue = [&](int i, int slot) {
         const int p = z0 - 1 + i;
-        const int slot = i % R;
         float* st = smf + (size_t)slot * L.floats;
         uint64_t* bar = bars + slot;
         const bool inner = i >= 1 && i <= nloc - 2;
@@ -467,7 +482,7 @@ __global__ void __launch_bounds__(TXV* TY) k_adjoint_tma(const AdjArgs a, const 
     __syncthreads();
     const int npro = min(R, nloc);
     if (tid == 0)
-        for (int i = 0; i < npro; ++i) issue(i);
+        for (int i = 0; i < npro; ++i) issue(i, i);
     int issued = npro;
 
     const int tile = blockIdx.x + g.ntiles_x * blockIdx.y;
@@ -486,14 +501,18 @@ __global__ void __launch_bounds__(TXV* TY) k_adjoint_tma(const AdjArgs a, const 
         return st[L.o_S + row * SH + 4 + (lf >> logC)] * st[row * SR + HF + lf];
     };
 
-    bool ok = wait_stage(bars, 0, R);
-    ok = wait_stage(bars, 1, R) && ok;
+    int s_m = 0, s_c = 1, s_p = 2 % R;
+    uint32_t ph_p = (R == 2) ? 1u : 0u;
+    bool ok = wait_bar(bars + 0, 0u);
+    ok = wait_bar(bars + 1, 0u) && ok;
+    float* lk_ptr = a.lk + (long long)z0 * g.PP + ro;
+    double* g_row = has_g ? a.gacc + (long long)z0 * g.CPP + (long long)y * g.nxs + x0c : nullptr;
     for (int z = z0; z < z1; ++z) {
         const int im = z - z0;
-        ok = wait_stage(bars, im + 2, R) && ok;
-        const float* sm_m = smf + (size_t)(im % R) * L.floats;
-        const float* sm_c = smf + (size_t)((im + 1) % R) * L.floats;
-        const float* sm_p = smf + (size_t)((im + 2) % R) * L.floats;
+        ok = wait_bar(bars + s_p, ph_p) && ok;
+        const float* sm_m = smf + (size_t)s_m * L.floats;
+        const float* sm_c = smf + (size_t)s_c * L.floats;
+        const float* sm_p = smf + (size_t)s_p * L.floats;
         const int lf = 4 * tx;
         const float4 qc = qv4(sm_c, r, lf);
         float4 xm, xp;
@@ -545,13 +564,15 @@ __global__ void __launch_bounds__(TXV* TY) k_adjoint_tma(const AdjArgs a, const 
             }
             rnz = ri < re ? a.r_ent[ri].z : 0x7fffffff;
         }
-        if (own) st4(a.lk + z * g.PP + ro, make_float4(lk[0], lk[1], lk[2], lk[3]));
+        if (own) st4(lk_ptr, make_float4(lk[0], lk[1], lk[2], lk[3]));
+        lk_ptr += g.PP;
         if (has_g) {
             float pr[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) pr[q] = own ? lk[q] * comp(d2v, q) : 0.f;
             const double* gs = reinterpret_cast<const double*>(sm_c + L.o_g) + ty * cells;
-            double* grow = a.gacc + z * g.CPP + (long long)y * g.nxs + x0c;
+            double* grow = g_row;
+            g_row += g.CPP;
             if (logC == 0) {
                 if (own) {
                     const int c0 = lf;
@@ -578,9 +599,12 @@ __global__ void __launch_bounds__(TXV* TY) k_adjoint_tma(const AdjArgs a, const 
         if (!ok) break;
         if (tid == 0 && im + R < nloc) {
             fence_proxy_async();
-            issue(im + R);
+            issue(im + R, s_m);
         }
         if (im + R < nloc) issued = im + R + 1;
+        s_m = s_c;
+        s_c = s_p;
+        if (++s_p == R) { s_p = 0; ph_p ^= 1u; }
     }
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);

@@ -1,0 +1,353 @@
+"""Continuous-batching service for forward and gradient FMC requests.
+
+Requests of different grids, element counts and kinds (forward-only or L2
+gradient) arrive over time.  The scheduler admits a request as soon as a slot
+is free and its device footprint (model + batch workspaces + its data, from
+the engine's own size queries) fits the HBM budget; requests that do not fit
+wait while later, smaller ones may go ahead; a request larger than the whole
+budget is rejected at once.  Each admitted request gets its own plan, its own
+workspaces and its own CUDA stream, so the batch sweeps of co-admitted
+requests overlap on the device; the request's shots advance C at a time in one
+launch per time step.  Wavefields and checkpoints stay on the device; only the
+request's inputs and its result cross PCIe/C2C.
+
+Latency is measured from a request's arrival to its result being on the host;
+``Stats`` gives p50/p99 and shots/s.  The scheduling logic is independent of
+the executor (``GpuExecutor`` here), so it is tested on the CPU with a fake.
+"""
+
+from __future__ import annotations
+
+import heapq
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+
+
+@dataclass
+class Request:
+    kind: str                      # "forward" | "gradient"
+    m: np.ndarray                  # squared slowness on the grid
+    geom: object                   # .idx of grid-index tuples
+    wavelet: np.ndarray
+    dt: float
+    h: float
+    nt: int
+    dobs: np.ndarray | None = None
+    src_list: list | None = None
+    footprints: list | None = None
+    sponge: np.ndarray | None = None
+    arrival: float = 0.0           # seconds after the stream starts
+    rid: int = -1
+    batch: int | None = None
+
+    @property
+    def n_shots(self):
+        return len(self.src_list) if self.src_list is not None else len(self.geom.idx)
+
+
+@dataclass
+class Result:
+    rid: int
+    kind: str
+    ok: bool
+    error: str | None = None
+    traces: np.ndarray | None = None
+    J: float | None = None
+    g: np.ndarray | None = None
+    shots: int = 0
+    footprint: int = 0
+    t_arrival: float = 0.0
+    t_admit: float = 0.0
+    t_done: float = 0.0
+
+    @property
+    def latency(self):
+        return self.t_done - self.t_arrival
+
+
+@dataclass
+class Stats:
+    n: int
+    ok: int
+    rejected: int
+    p50_s: float
+    p99_s: float
+    mean_s: float
+    makespan_s: float
+    shots: int
+    shots_per_s: float
+    max_concurrent: int
+    peak_reserved_bytes: int
+
+    def as_dict(self):
+        return dict(self.__dict__)
+
+
+def percentile(xs, q):
+    if not xs:
+        return float("nan")
+    xs = sorted(xs)
+    k = (len(xs) - 1) * q / 100.0
+    lo, hi = int(np.floor(k)), int(np.ceil(k))
+    return xs[lo] + (xs[hi] - xs[lo]) * (k - lo)
+
+
+class GpuExecutor:
+    """Runs one request on the GB300 engine on its own stream."""
+
+    def __init__(self, device=None, graphs=False):
+        import torch
+        self.torch = torch
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.graphs = graphs
+
+    def plan_for(self, req):
+        from .backend import Plan, choose_batch
+        from .geometry import element_csr
+        shape = tuple(req.m.shape)
+        tx, rx = element_csr(req.geom, shape, req.src_list, req.footprints)
+        mode = _lib.MODE_GRADIENT if req.kind == "gradient" else _lib.MODE_FORWARD
+        C = req.batch or choose_batch(shape, req.nt, tx.rows, rx.rows, len(rx.cell), 0, mode,
+                                      1 << 62)
+        C = min(C, 32)
+        plan = Plan(shape, req.h, req.dt, req.nt, tx, rx, batch=C)
+        if not self.graphs:
+            plan.set("graphs", 0)
+        return plan
+
+    def footprint(self, req, plan):
+        mode = _lib.MODE_GRADIENT if req.kind == "gradient" else _lib.MODE_FORWARD
+        data = 4 * plan.n_tx * plan.nt * plan.n_rx
+        cells = int(np.prod(plan.shape))
+        return plan.model_bytes() + plan.batch_bytes(mode) + data + 16 * cells + (1 << 20)
+
+    def run(self, req, plan):
+        torch = self.torch
+        from .backend import _ptr, _stream
+        lib = plan._lib
+        dev = self.device
+        st = torch.cuda.Stream(device=dev)
+        with torch.cuda.stream(st):
+            m = torch.from_numpy(np.ascontiguousarray(req.m, np.float64)).to(dev, non_blocking=True)
+            w = torch.from_numpy(np.ascontiguousarray(req.wavelet, np.float64)).to(dev)
+            sp = None if req.sponge is None else torch.from_numpy(
+                np.ascontiguousarray(req.sponge, np.float64)).to(dev)
+            mws = torch.empty(plan.model_bytes(), dtype=torch.uint8, device=dev)
+            s = _stream(st)
+            if req.kind == "forward":
+                bws = torch.empty(plan.batch_bytes(_lib.MODE_FORWARD), dtype=torch.uint8, device=dev)
+                data = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev)
+                _lib.check(lib.usct_forward_fmc_dev(plan.handle, _ptr(m), _ptr(sp), _ptr(w),
+                                                    _ptr(data), _ptr(mws), _ptr(bws), s))
+                plan.check(st)
+                return {"traces": data.cpu().numpy()}
+            dobs = torch.from_numpy(np.ascontiguousarray(req.dobs, np.float32)).to(dev)
+            bws = torch.empty(plan.batch_bytes(_lib.MODE_GRADIENT), dtype=torch.uint8, device=dev)
+            J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
+            g = torch.empty(plan.shape, dtype=torch.float64, device=dev)
+            _lib.check(lib.usct_misfit_and_gradient_dev(plan.handle, _ptr(m), _ptr(sp), _ptr(w),
+                                                        _ptr(dobs), _ptr(J), _ptr(g), _ptr(mws),
+                                                        _ptr(bws), s))
+            plan.check(st)
+            return {"J": float(J.sum().item()), "g": g.cpu().numpy()}
+
+    def release(self, plan):
+        plan.close()
+
+
+class Engine:
+    """Admission, slots and completion bookkeeping around an executor."""
+
+    def __init__(self, executor, budget_bytes, max_active=4):
+        self.ex = executor
+        self.budget = int(budget_bytes)
+        self.max_active = int(max_active)
+        self.lock = threading.Condition()
+        self.reserved = 0
+        self.active = 0
+        self.peak_reserved = 0
+        self.max_concurrent = 0
+
+    # -- one request ------------------------------------------------------------
+    def _worker(self, req, plan, fp, res, t0, on_done):
+        try:
+            out = self.ex.run(req, plan)
+            res.ok = True
+            res.traces = out.get("traces")
+            res.J = out.get("J")
+            res.g = out.get("g")
+        except Exception as exc:   # the request fails, the service goes on
+            res.ok = False
+            res.error = f"{type(exc).__name__}: {exc}"[:300]
+        finally:
+            try:
+                self.ex.release(plan)
+            except Exception:
+                pass
+            res.t_done = time.perf_counter() - t0
+            with self.lock:
+                self.reserved -= fp
+                self.active -= 1
+                self.lock.notify_all()
+            on_done(res)
+
+    # -- a whole stream ----------------------------------------------------------
+    def run_stream(self, requests, realtime=True):
+        """Replay ``requests`` (sorted by arrival) and return their Results in
+        request order.  With ``realtime`` the arrival times are honoured."""
+        reqs = sorted(enumerate(requests), key=lambda kv: kv[1].arrival)
+        results = [None] * len(requests)
+        pending = []          # (arrival, order, req, plan, fp)
+        threads = []
+        t0 = time.perf_counter()
+        done_count = [0]
+
+        def on_done(r):
+            with self.lock:
+                done_count[0] += 1
+                self.lock.notify_all()
+
+        nxt = 0
+        while True:
+            now = time.perf_counter() - t0
+            # arrivals
+            while nxt < len(reqs) and (not realtime or reqs[nxt][1].arrival <= now):
+                i, rq = reqs[nxt]
+                rq.rid = i
+                res = Result(rid=i, kind=rq.kind, ok=False, shots=rq.n_shots,
+                             t_arrival=rq.arrival if realtime else now)
+                results[i] = res
+                try:
+                    plan = self.ex.plan_for(rq)
+                    fp = int(self.ex.footprint(rq, plan))
+                except Exception as exc:
+                    res.error = f"{type(exc).__name__}: {exc}"[:300]
+                    res.t_done = res.t_admit = now
+                    with self.lock:
+                        done_count[0] += 1
+                    nxt += 1
+                    continue
+                res.footprint = fp
+                if fp > self.budget:
+                    res.error = (f"rejected: needs {fp} bytes of device memory, the budget is "
+                                 f"{self.budget}")
+                    res.t_done = res.t_admit = now
+                    self.ex.release(plan)
+                    with self.lock:
+                        done_count[0] += 1
+                else:
+                    heapq.heappush(pending, (res.t_arrival, i, rq, plan, fp))
+                nxt += 1
+            # admissions: first come first served, later ones may pass a head that
+            # does not fit yet
+            with self.lock:
+                keep = []
+                while pending:
+                    item = heapq.heappop(pending)
+                    _, i, rq, plan, fp = item
+                    if self.active < self.max_active and self.reserved + fp <= self.budget:
+                        self.reserved += fp
+                        self.active += 1
+                        self.peak_reserved = max(self.peak_reserved, self.reserved)
+                        self.max_concurrent = max(self.max_concurrent, self.active)
+                        res = results[i]
+                        res.t_admit = time.perf_counter() - t0
+                        th = threading.Thread(target=self._worker,
+                                              args=(rq, plan, fp, res, t0, on_done), daemon=True)
+                        threads.append(th)
+                        th.start()
+                    else:
+                        keep.append(item)
+                for item in keep:
+                    heapq.heappush(pending, item)
+                if done_count[0] == len(reqs):
+                    break
+                wait = None
+                if nxt < len(reqs) and realtime:
+                    wait = max(0.0, reqs[nxt][1].arrival - (time.perf_counter() - t0))
+                self.lock.wait(timeout=wait if wait is not None else 0.05)
+        for th in threads:
+            th.join()
+        return results
+
+
+def summarize(results, engine=None):
+    ok = [r for r in results if r.ok]
+    lat = [r.latency for r in ok]
+    t_first = min((r.t_arrival for r in results), default=0.0)
+    t_last = max((r.t_done for r in ok), default=0.0)
+    span = max(t_last - t_first, 1e-9)
+    shots = sum(r.shots for r in ok)
+    return Stats(n=len(results), ok=len(ok),
+                 rejected=sum(1 for r in results if not r.ok and r.error and
+                              r.error.startswith("rejected")),
+                 p50_s=percentile(lat, 50), p99_s=percentile(lat, 99),
+                 mean_s=float(np.mean(lat)) if lat else float("nan"), makespan_s=span,
+                 shots=shots, shots_per_s=shots / span,
+                 max_concurrent=engine.max_concurrent if engine else 0,
+                 peak_reserved_bytes=engine.peak_reserved if engine else 0)
+
+
+# ---------------------------------------------------------------------------
+# seeded request streams with the serving configuration's mix
+# ---------------------------------------------------------------------------
+def make_stream(n_requests, rate_hz, seed=0, sizes_2d=(128, 1024), sizes_3d=(96, 256),
+                elements_2d=(32, 256), elements_3d=(64, 512), frac_3d=0.5, frac_gradient=0.3,
+                nt_cap=None, dobs_fn=None):
+    """Poisson arrivals at ``rate_hz``; each request a 2D ring or 3D cylinder
+    problem (disc or random-field model), forward-only or gradient (then
+    ``dobs_fn(true_problem)`` supplies the observed data).  nt follows the
+    builder's rule t_end = 2.2 * 2R / 1450 with R = 0.8 x half the domain."""
+    from . import problems
+    from .geometry import CylinderGeometry, RingGeometry, ricker
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for k in range(n_requests):
+        t += rng.exponential(1.0 / rate_hz)
+        is3d = rng.uniform() < frac_3d
+        kind = "gradient" if rng.uniform() < frac_gradient else "forward"
+        if is3d:
+            n = int(rng.integers(sizes_3d[0] // 8, sizes_3d[1] // 8 + 1)) * 8
+            h = 0.2e-3
+            ne = int(rng.integers(elements_3d[0] // 8, elements_3d[1] // 8 + 1)) * 8
+            rings = 2 if ne < 128 else 4
+            R = 0.8 * (n - 1) * h / 2
+            geom = CylinderGeometry(rings, ne // rings, R, 0.5 * (n - 1) * h, (n - 1) * h, h)
+            shape = (n, n, n)
+        else:
+            n = int(rng.integers(sizes_2d[0] // 16, sizes_2d[1] // 16 + 1)) * 16
+            h = 0.15e-3
+            ne = int(rng.integers(elements_2d[0] // 8, elements_2d[1] // 8 + 1)) * 8
+            R = 0.8 * (n - 1) * h / 2
+            geom = RingGeometry(ne, R, (n - 1) * h, h)
+            shape = (n, n)
+        if rng.uniform() < 0.5:
+            f = problems.random_field(shape, 0.002 / h, 0.03, rng)
+            c = 1500.0 * (1.0 + f)
+        else:
+            c = np.full(shape, 1500.0)
+            centre = (n - 1) * h / 2
+            grids = np.meshgrid(*[np.arange(s) * h for s in shape], indexing="ij")
+            for rad, cv in ((0.25 * R, 1450.0), (0.35 * R, 1580.0)):
+                off = rng.uniform(-0.3 * R, 0.3 * R, size=len(shape))
+                r2 = sum((gx - centre - o) ** 2 for gx, o in zip(grids, off))
+                c[r2 <= rad * rad] = cv
+        dt = 0.3 * h / float(c.max())
+        nt = int(np.ceil(2.2 * 2 * R / 1450.0 / dt))
+        if nt_cap:
+            nt = min(nt, nt_cap)
+        wav = ricker(nt, dt, 1e6)
+        m_true = 1.0 / c ** 2
+        req = Request(kind=kind, m=m_true, geom=geom, wavelet=wav, dt=dt, h=h, nt=nt,
+                      arrival=t)
+        if kind == "gradient":
+            req.m = np.full(shape, 1.0 / 1500.0 ** 2)
+            req.dobs = dobs_fn(m_true, geom, wav, dt, h, nt) if dobs_fn else None
+        out.append(req)
+    return out

@@ -1,0 +1,115 @@
+"""GPU: the autograd operator, CUDA-graph replay and the serving engine."""
+
+import numpy as np
+import pytest
+
+import oracle
+from golden_util import load, rel_l2
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def cuda():
+    assert torch.cuda.is_available()
+    from openusct_gb300 import build
+    build.build()
+
+
+def test_autograd_l2_gradient_equals_misfit_and_gradient():
+    import openusct_gb300.backend as gb
+    from openusct_gb300.autograd import FMCProblem, fmc
+    c = load("gpu3d")
+    sl = c.src_list[:6]
+    dobs = torch.from_numpy(c["dobs"][:6]).float().cuda()
+    for keep in (None, 0):   # checkpoints kept from the forward / recomputed in backward
+        prob = FMCProblem(c["m0"].shape, c.geom, c.wavelet, c.dt, c.h, c.nt, src_list=sl,
+                          batch=4, ckpt_k=16, keep_bytes=keep)
+        m = torch.from_numpy(c["m0"]).cuda().requires_grad_(True)
+        tr = fmc(m, prob)
+        loss = 0.5 * ((tr - dobs) ** 2).double().sum()
+        loss.backward()
+        J, g = gb.misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"][:6],
+                                      src_list=sl, batch=4, ckpt_k=16)
+        assert np.array_equal(m.grad.cpu().numpy(), g)
+        assert abs(loss.item() - J) <= 1e-9 * J
+
+
+def test_autograd_slowness_parametrisation_matches_fd():
+    from openusct_gb300.autograd import FMCProblem, fmc
+    c = load("parity3d")
+    sl = c.src_list[:2]
+    dobs = c["dobs"][:2]
+    s0 = np.sqrt(c["m0"])
+    prob = FMCProblem(s0.shape, c.geom, c.wavelet, c.dt, c.h, c.nt, src_list=sl, batch=2)
+    s = torch.from_numpy(s0).cuda().requires_grad_(True)
+    tr = fmc(s, prob, param="slowness")
+    loss = 0.5 * ((tr - torch.from_numpy(dobs).float().cuda()) ** 2).double().sum()
+    loss.backward()
+    gs = s.grad.cpu().numpy()
+    rng = np.random.default_rng(4)
+    for _ in range(3):
+        ds = rng.standard_normal(s0.shape)
+        ds[:3] = ds[-3:] = ds[:, :3] = ds[:, -3:] = ds[:, :, :3] = ds[:, :, -3:] = 0.0
+        ds *= float(np.mean(s0))
+        eps = 1e-6
+        Jp = oracle.misfit((s0 + eps * ds) ** 2, c.geom, c.wavelet, c.dt, c.h, c.nt, dobs,
+                           src_list=sl)
+        Jm = oracle.misfit((s0 - eps * ds) ** 2, c.geom, c.wavelet, c.dt, c.h, c.nt, dobs,
+                           src_list=sl)
+        fd = (Jp - Jm) / (2 * eps)
+        assert abs(float(np.sum(gs * ds)) - fd) <= 1e-4 * abs(fd)
+
+
+def test_graph_replay_is_bit_identical():
+    import openusct_gb300.backend as gb
+    c = load("parity2d")
+    base = dict(src_list=c.src_list, batch=8, ckpt_k=20)
+    J0, g0 = gb.misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                                    tile=(128, 1, 0, 1), **base)
+    plan = gb._PLANS[next(reversed(gb._PLANS))]
+    plan.set("graphs", 1)
+    outs = [gb.misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                                   tile=(128, 1, 0, 1), **base) for _ in range(3)]
+    for J, g in outs:
+        assert J == J0 and np.array_equal(g, g0)
+    # a different model through the same captured graphs
+    m1 = c["m0"] * 1.01
+    J1, g1 = gb.misfit_and_gradient(m1, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                                    tile=(128, 1, 0, 1), **base)
+    plan.set("graphs", 0)
+    J2, g2 = gb.misfit_and_gradient(m1, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                                    tile=(128, 1, 0, 1), **base)
+    assert J1 == J2 and np.array_equal(g1, g2)
+
+
+def test_each_result_is_the_same_alone_and_in_the_mix():
+    import openusct_gb300.backend as gb
+    from openusct_gb300.serve import Engine, GpuExecutor, make_stream, summarize
+
+    def dobs_fn(m, geom, wav, dt, h, nt):
+        return gb.forward_fmc(m, geom, wav, dt, h, nt)
+
+    reqs = make_stream(8, rate_hz=40.0, seed=3, sizes_2d=(96, 160), sizes_3d=(40, 56),
+                       elements_2d=(16, 32), elements_3d=(16, 32), frac_gradient=0.5,
+                       nt_cap=300, dobs_fn=dobs_fn)
+    eng = Engine(GpuExecutor(), budget_bytes=40 << 30, max_active=4)
+    mixed = eng.run_stream(reqs)
+    st = summarize(mixed, eng)
+    assert st.ok == len(reqs)
+    assert eng.max_concurrent >= 2
+    alone = Engine(GpuExecutor(), budget_bytes=40 << 30, max_active=1).run_stream(
+        reqs, realtime=False)
+    for a, b in zip(mixed, alone):
+        assert a.ok and b.ok
+        if a.kind == "forward":
+            assert np.array_equal(a.traces, b.traces)
+        else:
+            assert a.J == b.J and np.array_equal(a.g, b.g)
+    # and agree with the backend's own call (its batch width may differ, which
+    # only re-associates the FP32 shot sum of the imaging condition)
+    for r, q in zip(mixed, reqs):
+        if q.kind == "gradient":
+            J, g = gb.misfit_and_gradient(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt, q.dobs)
+            assert rel_l2(r.g, g) < 1e-5 and abs(r.J - J) <= 1e-9 * abs(J)

@@ -1,0 +1,111 @@
+"""Serving scheduler logic on the CPU (a fake executor stands in for the GPU)."""
+
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from openusct_gb300.serve import Engine, Request, percentile, summarize
+
+
+class FakePlan:
+    def __init__(self, fp, dur, fail=False):
+        self.fp, self.dur, self.fail = fp, dur, fail
+
+
+class FakeExecutor:
+    """Footprint and run time come from the request's ``m`` (a 3-vector)."""
+
+    def __init__(self):
+        self.lock = threading.Lock()
+        self.running = 0
+        self.peak = 0
+        self.released = 0
+
+    def plan_for(self, req):
+        fp, dur, fail = req.m
+        if fp < 0:
+            raise ValueError("bad request")
+        return FakePlan(int(fp), float(dur), bool(fail))
+
+    def footprint(self, req, plan):
+        return plan.fp
+
+    def run(self, req, plan):
+        with self.lock:
+            self.running += 1
+            self.peak = max(self.peak, self.running)
+        time.sleep(plan.dur)
+        with self.lock:
+            self.running -= 1
+        if plan.fail:
+            raise RuntimeError("injected device failure")
+        return {"J": float(plan.fp)}
+
+    def release(self, plan):
+        with self.lock:
+            self.released += 1
+
+
+def req(fp, dur, arrival=0.0, fail=False):
+    return Request(kind="gradient", m=(fp, dur, fail), geom=type("G", (), {"idx": [0, 1]})(),
+                   wavelet=None, dt=1.0, h=1.0, nt=2, arrival=arrival)
+
+
+def test_admission_never_exceeds_the_budget_and_requests_overlap():
+    ex = FakeExecutor()
+    eng = Engine(ex, budget_bytes=100, max_active=8)
+    rs = eng.run_stream([req(40, 0.15, 0.0), req(40, 0.15, 0.01), req(40, 0.15, 0.02),
+                         req(30, 0.05, 0.03)])
+    assert all(r.ok for r in rs)
+    assert eng.peak_reserved <= 100
+    assert eng.max_concurrent >= 2 and ex.peak >= 2
+    assert ex.released == 4
+
+
+def test_request_larger_than_budget_is_rejected_immediately():
+    ex = FakeExecutor()
+    eng = Engine(ex, budget_bytes=100, max_active=2)
+    rs = eng.run_stream([req(500, 0.01, 0.0), req(50, 0.01, 0.0)])
+    assert not rs[0].ok and rs[0].error.startswith("rejected")
+    assert rs[0].latency < 0.05
+    assert rs[1].ok
+
+
+def test_smaller_request_passes_a_blocked_head():
+    ex = FakeExecutor()
+    eng = Engine(ex, budget_bytes=100, max_active=4)
+    # a long 60-byte job runs; a 60-byte head must wait; a 30-byte one can go ahead
+    rs = eng.run_stream([req(60, 0.3, 0.0), req(60, 0.05, 0.02), req(30, 0.05, 0.04)])
+    assert all(r.ok for r in rs)
+    assert rs[2].t_admit < rs[1].t_admit
+
+
+def test_a_failing_request_does_not_stop_the_service():
+    ex = FakeExecutor()
+    eng = Engine(ex, budget_bytes=100, max_active=2)
+    rs = eng.run_stream([req(10, 0.02, 0.0, fail=True), req(10, 0.02, 0.0), req(-1, 0.0, 0.0)])
+    assert not rs[0].ok and "injected" in rs[0].error
+    assert rs[1].ok
+    assert not rs[2].ok and "bad request" in rs[2].error
+    assert eng.reserved == 0 and eng.active == 0
+
+
+def test_slots_cap_concurrency():
+    ex = FakeExecutor()
+    eng = Engine(ex, budget_bytes=10 ** 9, max_active=2)
+    eng.run_stream([req(1, 0.05, 0.0) for _ in range(6)])
+    assert ex.peak <= 2
+
+
+def test_percentiles_and_summary():
+    assert percentile([1, 2, 3, 4], 50) == pytest.approx(2.5)
+    assert percentile(list(range(101)), 99) == pytest.approx(99.0)
+    ex = FakeExecutor()
+    eng = Engine(ex, budget_bytes=100, max_active=4)
+    rs = eng.run_stream([req(10, 0.02, 0.01 * i) for i in range(8)])
+    st = summarize(rs, eng)
+    assert st.ok == 8 and st.shots == 16
+    assert st.p50_s <= st.p99_s
+    assert st.shots_per_s > 0
