@@ -166,15 +166,48 @@ __device__ __forceinline__ float4 cell4s(const float* row, int lf, int logC) {
     return make_float4(s, s, s, s);
 }
 
+// Paired FP32 arithmetic on float4 (two lanes per instruction on sm_100+).
+// Every lane is rounded exactly as the scalar operation would be, so results
+// stay bit-identical to the scalar op order of the oracle.
+__device__ __forceinline__ float2 lo2(const float4& a) { return make_float2(a.x, a.y); }
+__device__ __forceinline__ float2 hi2(const float4& a) { return make_float2(a.z, a.w); }
+__device__ __forceinline__ float4 cat4(const float2& l, const float2& h) {
+    return make_float4(l.x, l.y, h.x, h.y);
+}
+__device__ __forceinline__ float4 add4(const float4& a, const float4& b) {
+    return cat4(__fadd2_rn(lo2(a), lo2(b)), __fadd2_rn(hi2(a), hi2(b)));
+}
 __device__ __forceinline__ float4 mul4(const float4& a, const float4& b) {
-    return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w);
+    return cat4(__fmul2_rn(lo2(a), lo2(b)), __fmul2_rn(hi2(a), hi2(b)));
+}
+__device__ __forceinline__ float4 fma4(const float4& a, const float4& b, const float4& c) {
+    return cat4(__ffma2_rn(lo2(a), lo2(b), lo2(c)), __ffma2_rn(hi2(a), hi2(b), hi2(c)));
+}
+__device__ __forceinline__ float4 neg4(const float4& a) { return make_float4(-a.x, -a.y, -a.z, -a.w); }
+__device__ __forceinline__ float4 splat4(float v) { return make_float4(v, v, v, v); }
+__device__ __forceinline__ float4 sel4(const bool in[4], const float4& a) {
+    return make_float4(in[0] ? a.x : 0.f, in[1] ? a.y : 0.f, in[2] ? a.z : 0.f, in[3] ? a.w : 0.f);
+}
+// The stencil of usct_kernels.cuh's stencil(), four lanes at once:
+// lap = fma(cen, c, ((x- + x+) [+ (y- + y+)]) + (z- + z+)) * inv_h2, 0 off the interior.
+__device__ __forceinline__ float4 stencil4(const bool in[4], float cen, const float4& c,
+                                           const float4& xm, const float4& xp, const float4& ym,
+                                           const float4& yp, const float4& zm, const float4& zp,
+                                           bool is3d, float inv_h2) {
+    float4 t = add4(xm, xp);
+    if (is3d) t = add4(t, add4(ym, yp));
+    t = add4(t, add4(zm, zp));
+    return sel4(in, mul4(fma4(splat4(cen), c, t), splat4(inv_h2)));
+}
+__device__ __forceinline__ void put4(float* d, const float4& v) {
+    d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
 }
 
 // ---------------------------------------------------------------------------
 // forward step, TMA ring
 // ---------------------------------------------------------------------------
 template <int TXV, int TY, bool IS3D, bool BORN>
-__global__ void __launch_bounds__(TXV* TY) k_forward_tma(const FwdArgs a, const __grid_constant__ FwdMaps mp,
+__global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : ((TXV * TY >= 256) ? 4 : 8)) k_forward_tma(const FwdArgs a, const __grid_constant__ FwdMaps mp,
                                                          const int R, int* err) {
     extern __shared__ __align__(128) float smf[];
     const Geo& g = a.g;
@@ -300,11 +333,11 @@ __global__ void __launch_bounds__(TXV* TY) k_forward_tma(const FwdArgs a, const 
         const float4 Sv = cell4s(sm_c + L.o_S + ty * cells, 4 * tx, logC);
         const float4 spv = has_sp ? cell4s(sm_c + L.o_sp + ty * cells, 4 * tx, logC) : f4zero();
         const bool zy_in = y_in && z >= 1 && z <= g.nz - 2;
-        float lap[4];
+        bool in[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-            lap[q] = stencil(zy_in && x_in[q], cen, comp(cc, q), comp(xm, q), comp(xp, q),
-                             comp(ym, q), comp(yp, q), comp(cm, q), comp(cp, q), IS3D, inv_h2);
+        for (int q = 0; q < 4; ++q) in[q] = zy_in && x_in[q];
+        float lap[4];
+        put4(lap, stencil4(in, cen, cc, xm, xp, ym, yp, cm, cp, IS3D, inv_h2));
         if (z == snz) {
             while (si < se) {
                 const SrcEnt e = a.s_ent[si];
@@ -319,16 +352,14 @@ __global__ void __launch_bounds__(TXV* TY) k_forward_tma(const FwdArgs a, const 
             }
             snz = si < se ? a.s_ent[si].z : 0x7fffffff;
         }
+        // p^n = fma(S, lap, 2c - p^{n-2}) with 2c - p computed as fma(2, c, -p) (2c is exact)
+        float4 v4 = fma4(Sv, make_float4(lap[0], lap[1], lap[2], lap[3]),
+                         fma4(splat4(2.f), cc, neg4(ppv)));
+        if (has_sp) v4 = mul4(v4, spv);
         float pn[4], d2v[4], out[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float c = comp(cc, q);
-            float v = __fmaf_rn(comp(Sv, q), lap[q], 2.f * c - comp(ppv, q));
-            if (has_sp) v = v * comp(spv, q);
-            d2v[q] = (v - 2.f * c) + comp(ppv, q);
-            pn[q] = v;
-            out[q] = v;
-        }
+        put4(pn, v4);
+        put4(out, v4);
+        if (BORN || d2_ptr) put4(d2v, add4(fma4(splat4(-2.f), cc, v4), ppv));   // (p^n - 2c) + p
         if (BORN) {
             const float* dcs = sm_c + L.o_dc;
             const float4 dcc = ld4(dcs + r * SR + col);
@@ -343,19 +374,12 @@ __global__ void __launch_bounds__(TXV* TY) k_forward_tma(const FwdArgs a, const 
             const float4 dp = ld4(sm_p + L.o_dc + r * SR + col);
             const float4 dppv = ld4(sm_c + L.o_dpp + ty * TXF + 4 * tx);
             const float4 vmv = cell4s(sm_c + L.o_vm + ty * cells, 4 * tx, logC);
-            float dv[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float dl = stencil(zy_in && x_in[q], cen, comp(dcc, q), comp(dxm, q),
-                                         comp(dxp, q), comp(dym, q), comp(dyp, q), comp(dm, q),
-                                         comp(dp, q), IS3D, inv_h2);
-                float v = __fmaf_rn(comp(Sv, q), dl, 2.f * comp(dcc, q) - comp(dppv, q));
-                v = __fmaf_rn(-comp(vmv, q), d2v[q], v);
-                if (has_sp) v = v * comp(spv, q);
-                dv[q] = v;
-                out[q] = v;
-            }
-            if (own) st4(dn_ptr, make_float4(dv[0], dv[1], dv[2], dv[3]));
+            const float4 dl = stencil4(in, cen, dcc, dxm, dxp, dym, dyp, dm, dp, IS3D, inv_h2);
+            float4 dv = fma4(Sv, dl, fma4(splat4(2.f), dcc, neg4(dppv)));
+            dv = fma4(neg4(vmv), make_float4(d2v[0], d2v[1], d2v[2], d2v[3]), dv);
+            if (has_sp) dv = mul4(dv, spv);
+            put4(out, dv);
+            if (own) st4(dn_ptr, dv);
         }
         if (own) {
             const float4 v = make_float4(pn[0], pn[1], pn[2], pn[3]);
@@ -538,16 +562,15 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
         const float4 d2v = ld4(sm_c + L.o_d2 + ty * TXF + lf);
         const float4 spv = has_sp ? cell4s(sm_c + L.o_sp + ty * cells, lf, logC) : f4zero();
         const bool zy_in = y_in && z >= 1 && z <= g.nz - 2;
-        float lk[4];
+        bool in[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float lq = stencil(zy_in && x_in[q], cen, comp(qc, q), comp(xm, q), comp(xp, q),
-                                     comp(ym, q), comp(yp, q), comp(qm, q), comp(qp, q), IS3D,
-                                     inv_h2);
-            float v = (2.f * comp(l1c, q) - comp(l2v, q)) + lq;
-            if (has_sp) v = v * comp(spv, q);
-            lk[q] = v;
-        }
+        for (int q = 0; q < 4; ++q) in[q] = zy_in && x_in[q];
+        // lam^k = (2 lam^{k+1} - lam^{k+2}) + L q, with 2l - l2 as fma(2, l, -l2)
+        const float4 lq = stencil4(in, cen, qc, xm, xp, ym, yp, qm, qp, IS3D, inv_h2);
+        float4 lk4 = add4(fma4(splat4(2.f), l1c, neg4(l2v)), lq);
+        if (has_sp) lk4 = mul4(lk4, spv);
+        float lk[4];
+        put4(lk, lk4);
         if (z == rnz) {
             while (ri < re) {
                 const RxEnt e = a.r_ent[ri];
@@ -568,8 +591,7 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
         lk_ptr += g.PP;
         if (has_g) {
             float pr[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) pr[q] = own ? lk[q] * comp(d2v, q) : 0.f;
+            put4(pr, own ? mul4(make_float4(lk[0], lk[1], lk[2], lk[3]), d2v) : f4zero());
             const double* gs = reinterpret_cast<const double*>(sm_c + L.o_g) + ty * cells;
             double* grow = g_row;
             g_row += g.CPP;

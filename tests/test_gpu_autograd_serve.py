@@ -28,7 +28,7 @@ def test_autograd_l2_gradient_equals_misfit_and_gradient():
                           batch=4, ckpt_k=16, keep_bytes=keep)
         m = torch.from_numpy(c["m0"]).cuda().requires_grad_(True)
         tr = fmc(m, prob)
-        loss = 0.5 * ((tr - dobs) ** 2).double().sum()
+        loss = 0.5 * ((tr - dobs).double() ** 2).sum()
         loss.backward()
         J, g = gb.misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"][:6],
                                       src_list=sl, batch=4, ckpt_k=16)
