@@ -298,13 +298,17 @@ def main():
     t_launch = e0.elapsed_time(e1) / 1000.0 / (nrep * (prob.nt - 1))
     fwd_bytes = (12 * C + 4) * cells
     achieved = fwd_bytes / t_launch / 1e9
+    # DRAM traffic of the same kernel from the committed ncu capture of a smaller
+    # case (128^3, 16 shots), scaled by cell-channels to this launch
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "k_forward_traffic.json")
+    prof = os.path.join(ROOT, "profiles", "k_forward_tma_128cube_C16.md")
     if os.path.exists(prof):
         try:
-            with open(prof) as f:
-                pj = json.load(f)
-            traffic = float(pj["dram_bytes_per_launch"]) * (cells * C) / float(pj["cell_channels"])
+            kv = {}
+            for line in open(prof):
+                if ":" in line and line.split(":")[0] in ("dram_bytes_per_launch", "cell_channels"):
+                    kv[line.split(":")[0]] = float(line.split(":")[1])
+            traffic = kv["dram_bytes_per_launch"] * (cells * C) / kv["cell_channels"]
         except Exception:
             traffic = None
 
@@ -387,7 +391,10 @@ def main():
             "roofline": {"bound": "hbm", "kernel": "k_forward (3D, batched)",
                          "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind,
-                         "traffic": traffic, "algorithmic_bytes_per_launch": fwd_bytes,
+                         "traffic": traffic,
+                         "traffic_source": "profiles/k_forward_tma_128cube_C16.md, scaled by "
+                                           "cell-channels (128^3x16 -> this launch)",
+                         "algorithmic_bytes_per_launch": fwd_bytes,
                          "launch_ms": t_launch * 1000.0},
             "pipeline_roofline": {"bytes_per_step": pipeline_bytes,
                                   "achieved": pipeline_bytes / (t_ms / 1000.0) / 1e9,
