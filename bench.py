@@ -37,6 +37,25 @@ METRIC = "Grad shots/s + p50/p99, batched serve vs per-shot plain, same GB300, r
 WORKLOAD = ("3D acoustic cylinder FMC L2 gradient, 192^3, dx=0.2mm, 8x32 elements (256 shots), "
             "nt=2000, FP32, 32 shots per launch, checkpoint every 64 steps")
 
+# name -> (description, problem builder, shots per launch, checkpoint k, mode)
+#   mode "grad": one step = the L2 gradient of one batch (model: 44 B/shot + 20 B/batch
+#   per cell-step); "gn": one step = the Gauss-Newton product of one batch
+#   (44 + 12 B/shot + 24 B/batch)
+WORKLOADS = {
+    "grad3d": (WORKLOAD, lambda: __import__("openusct_gb300.problems").problems.cylinder3d(seed=0),
+               32, 64, "grad"),
+    "ring2d": ("2D ring FWI L2 gradient, 256^2, dx=0.15mm, 64-element ring r=16mm, two seeded "
+               "discs, 1 MHz Ricker, nt=1500, FP32, all 64 shots in one launch",
+               lambda: __import__("openusct_gb300.problems").problems.ring2d(seed=0), 64, 0, "grad"),
+    "gn3d": ("3D Gauss-Newton Hessian-vector product (Born + adjoint), 224^3, dx=0.18mm, 8x32 "
+             "elements (256 shots), nt=2500, FP32, 16 shots per launch",
+             lambda: __import__("openusct_gb300.problems").problems.gn3d(seed=0), 16, 0, "gn"),
+    "grad3d_large": ("3D cylinder FMC L2 gradient, 320^3, dx=0.12mm, 16x32 elements (512 shots), "
+                     "nt=3000, FP32, 8 shots per launch",
+                     lambda: __import__("openusct_gb300.problems").problems.cylinder3d_large(seed=0),
+                     8, 0, "grad"),
+}
+
 
 def _peaks():
     try:
@@ -96,21 +115,31 @@ class Clocks:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_gradient_sample(prob, shot, nt_sample, k):
-    """Time the FP64 oracle gradient for one shot over nt_sample levels and
-    scale to the full time axis: returns (shots/s, seconds, description)."""
+def cpu_gradient_sample(prob, shot, nt_sample, k, mode="grad"):
+    """Time the FP64 oracle gradient (or Gauss-Newton product) for one shot over
+    nt_sample levels and scale to the full time axis: (shots/s, seconds, text)."""
     import numpy as np
     import oracle
+    nt_sample = min(nt_sample, prob.nt)
     wav = prob.wavelet[:nt_sample]
     geom = prob.geom
+    if mode == "gn":
+        t0 = time.perf_counter()
+        oracle.gn_hessian_vector(prob.m0, geom, wav, prob.dt, prob.h, nt_sample, prob.v,
+                                 src_list=[shot], k=k)
+        dt_s = time.perf_counter() - t0
+        per_shot = dt_s * (prob.nt - 1) / (nt_sample - 1)
+        return 1.0 / per_shot, dt_s, (f"1 shot x {nt_sample} levels of the Gauss-Newton product "
+                                      f"(checkpoint k={k}), scaled by (nt-1)/{nt_sample - 1}")
     rec_all = oracle.forward_fmc(prob.m_true, geom, wav, prob.dt, prob.h, nt_sample, None, [shot])
     t0 = time.perf_counter()
     oracle.misfit_and_gradient(prob.m0, geom, wav, prob.dt, prob.h, nt_sample, rec_all, None,
                                [shot], k=k)
     dt_s = time.perf_counter() - t0
     per_shot = dt_s * (prob.nt - 1) / (nt_sample - 1)
-    return 1.0 / per_shot, dt_s, (f"1 shot x {nt_sample} levels of the {prob.shape[0]}^3 "
-                                  f"gradient (checkpoint k={k}), scaled by (nt-1)/{nt_sample - 1}")
+    grid = "x".join(str(v) for v in prob.shape)
+    return 1.0 / per_shot, dt_s, (f"1 shot x {nt_sample} levels of the {grid} gradient "
+                                  f"(checkpoint k={k}), scaled by (nt-1)/{nt_sample - 1}")
 
 
 SERVE_STREAM = ("seeded Poisson stream at 20 req/s, 30% gradient / 70% forward, half 2D rings "
@@ -166,16 +195,16 @@ def serve_phase(args):
             "speedup_vs_plain_sequential": (st.shots_per_s / plain_rate) if plain_rate else None}
 
 
-def run_reference(args, prob):
+def run_reference(args, prob, desc_w, mode):
     """--impl reference: the reference scheme's CPU path on the host cores."""
     import oracle
     oracle.build()
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     kind = "port"
-    nt_sample = 24
+    nt_sample = 24 if len(prob.shape) == 3 else 300
     vals = []
     for i in range(args.warmup + args.steps):
-        v, secs, desc = cpu_gradient_sample(prob, i % prob.n_shots, nt_sample, 8)
+        v, secs, desc = cpu_gradient_sample(prob, i % prob.n_shots, nt_sample, 8, mode)
         if i >= args.warmup:
             vals.append((v, secs))
     value = statistics.median(v for v, _ in vals)
@@ -184,7 +213,7 @@ def run_reference(args, prob):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "l2": "inputs larger than L2"},
+            "config": {"workload": desc_w, "l2": "inputs larger than L2"},
             "cpu_baseline": {"value": value, "unit": "shots/s", "cores": cores, "kind": kind,
                              "sample": desc},
             "e2e": {"value": value, "unit": "shots/s", "h2d_bytes_per_step": 0,
@@ -198,10 +227,11 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=192, help="grid size (default: the benchmark's 192)")
-    ap.add_argument("--nt", type=int, default=2000)
-    ap.add_argument("--batch", type=int, default=32)
-    ap.add_argument("--ckpt", type=int, default=64)
+    ap.add_argument("--workload", default="grad3d", choices=sorted(WORKLOADS))
+    ap.add_argument("--n", type=int, default=0, help="override the grid size (smaller variants)")
+    ap.add_argument("--nt", type=int, default=0, help="override the time levels")
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--ckpt", type=int, default=-1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
@@ -213,12 +243,18 @@ def main():
     import numpy as np
     from openusct_gb300 import problems
 
-    per_ring = 32
-    prob = problems.cylinder3d(seed=0, n=args.n, h=0.2e-3 * 191 / (args.n - 1), nt=args.nt,
-                               per_ring=per_ring)
+    desc_w, build_prob, C0, k0, mode = WORKLOADS[args.workload]
+    if args.n or args.nt:
+        if args.workload != "grad3d":
+            raise SystemExit("--n/--nt overrides apply to the grad3d workload only")
+        n = args.n or 192
+        prob = problems.cylinder3d(seed=0, n=n, h=0.2e-3 * 191 / (n - 1), nt=args.nt or 2000)
+        desc_w = f"{n}^3 nt={prob.nt} variant of: " + desc_w
+    else:
+        prob = build_prob()
     if args.impl == "reference":
         if rank == 0:
-            run_reference(args, prob)
+            run_reference(args, prob, desc_w, mode)
         return
 
     import torch
@@ -233,11 +269,13 @@ def main():
     from openusct_gb300.geometry import element_csr
     import ctypes
 
-    C = args.batch
-    # replicas: rank r owns the batches r, r+world, ...
-    shots = list(range(C * rank, C * rank + C))
+    C = args.batch or C0
+    ckpt = args.ckpt if args.ckpt >= 0 else k0
+    # replicas: rank r owns the batch of shots r*C .. r*C+C-1
+    shots = [(C * rank + i) % prob.n_shots for i in range(C)]
     tx, rx = element_csr(prob.geom, prob.shape, shots, None)
-    plan = backend.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx, rx, batch=C, ckpt_k=args.ckpt)
+    plan = backend.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx, rx, batch=C, ckpt_k=ckpt)
+    bmode = _lib.MODE_BORN if mode == "gn" else _lib.MODE_GRADIENT
     lib = _lib.load()
     s = torch.cuda.current_stream()
     sp = ctypes.c_void_p(s.cuda_stream)
@@ -247,17 +285,22 @@ def main():
     m0 = torch.from_numpy(prob.m0).to(dev)
     wav = torch.from_numpy(prob.wavelet).to(dev)
     mws = torch.empty(plan.model_bytes(), dtype=torch.uint8, device=dev)
-    bws = torch.empty(plan.batch_bytes(_lib.MODE_GRADIENT), dtype=torch.uint8, device=dev)
+    bws = torch.empty(plan.batch_bytes(bmode), dtype=torch.uint8, device=dev)
     dobs = torch.empty((C, prob.nt, plan.n_rx), dtype=torch.float32, device=dev)
     # observed data from the true model (same engine, forward only)
     _lib.check(lib.usct_forward_fmc_dev(plan.handle, P(m_true), None, P(wav), P(dobs), P(mws),
                                         P(bws), sp))
     J = torch.zeros(C, dtype=torch.float64, device=dev)
     g = torch.empty(prob.shape, dtype=torch.float64, device=dev)
+    vt = torch.from_numpy(prob.v).to(dev) if mode == "gn" else None
 
     def step():
-        _lib.check(lib.usct_misfit_and_gradient_dev(plan.handle, P(m0), None, P(wav), P(dobs),
-                                                    P(J), P(g), P(mws), P(bws), sp))
+        if mode == "gn":
+            _lib.check(lib.usct_gn_hessian_vector_dev(plan.handle, P(m0), None, P(wav), P(vt),
+                                                      P(g), None, P(mws), P(bws), sp))
+        else:
+            _lib.check(lib.usct_misfit_and_gradient_dev(plan.handle, P(m0), None, P(wav),
+                                                        P(dobs), P(J), P(g), P(mws), P(bws), sp))
 
     for _ in range(args.warmup):
         step()
@@ -282,7 +325,12 @@ def main():
     value = C * world / (t_ms / 1000.0)
     cells = int(np.prod(prob.shape))
     hbm, peak_kind = _peaks()
-    pipeline_bytes = (44 * C + 20) * cells * (prob.nt - 1)
+    if mode == "gn":
+        pipeline_bytes = (56 * C + 24) * cells * (prob.nt - 1)
+        pipeline_model = "56 B/shot + 24 B/batch per cell-step (Born + checkpointed adjoint)"
+    else:
+        pipeline_bytes = (44 * C + 20) * cells * (prob.nt - 1)
+        pipeline_model = "44 B/shot + 20 B/batch per cell-step"
 
     # dominant kernel: the forward stencil launch, timed live (forward-only sweep)
     fws = bws
@@ -320,21 +368,28 @@ def main():
     if rank == 0:
         m0_h = prob.m0
         dobs_h = dobs.double().cpu().numpy()
+        kw = dict(src_list=shots, batch=C, ckpt_k=ckpt or None)
+        call = (lambda: backend.gn_hessian_vector(m0_h, prob.geom, prob.wavelet, prob.dt, prob.h,
+                                                  prob.nt, prob.v, **kw)) if mode == "gn" else \
+            (lambda: backend.misfit_and_gradient(m0_h, prob.geom, prob.wavelet, prob.dt, prob.h,
+                                                 prob.nt, dobs_h, **kw)[1])
+        call()   # first call builds the plan (and, for small grids, captures graphs)
         t0 = time.perf_counter()
-        ne = 1
+        ne = 1 if cells * C > (1 << 24) else 5
         for _ in range(ne):
-            Jh, gh = backend.misfit_and_gradient(m0_h, prob.geom, prob.wavelet, prob.dt, prob.h,
-                                                 prob.nt, dobs_h, src_list=shots, batch=C,
-                                                 ckpt_k=args.ckpt)
+            gh = call()
         te = (time.perf_counter() - t0) / ne
-        e2e = {"value": C / te, "unit": "shots/s",
-               "h2d_bytes_per_step": int(m0_h.nbytes + C * prob.nt * plan.n_rx * 4 +
-                                         prob.wavelet.nbytes),
-               "d2h_bytes_per_step": int(gh.nbytes + 8 * C)}
+        h2d = m0_h.nbytes + prob.wavelet.nbytes + (prob.v.nbytes if mode == "gn" else
+                                                    C * prob.nt * plan.n_rx * 4)
+        e2e = {"value": C / te, "unit": "shots/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(gh.nbytes + (0 if mode == "gn" else 8 * C)),
+               "api": "openusct_gb300.backend." + ("gn_hessian_vector" if mode == "gn"
+                                                   else "misfit_and_gradient")}
+        backend.release()
 
     # plain one-shot-per-launch GPU form, same workload, one shot
     plain = None
-    if rank == 0 and not args.no_plain:
+    if rank == 0 and not args.no_plain and mode == "grad":
         backend._PLANS.clear()
         torch.cuda.empty_cache()
         tx1, rx1 = element_csr(prob.geom, prob.shape, [0], None)
@@ -355,7 +410,7 @@ def main():
         del pws
 
     serve = None
-    if rank == 0 and not args.no_serve:
+    if rank == 0 and not args.no_serve and args.workload == "grad3d":
         try:
             serve = serve_phase(args)
         except Exception as exc:   # reported, never fatal for the main line
@@ -366,7 +421,8 @@ def main():
         try:
             import oracle
             oracle.build()
-            v, secs, desc = cpu_gradient_sample(prob, 0, 40, 8)
+            v, secs, desc = cpu_gradient_sample(prob, 0, 40 if len(prob.shape) == 3 else 600, 8,
+                                                mode)
             cpu = {"value": v, "unit": "shots/s",
                    "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
                    "kind": "port", "sample": desc, "seconds": secs}
@@ -375,12 +431,12 @@ def main():
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": "shots/s", "n_gpus": world,
+            "metric": METRIC if mode == "grad" else "Gauss-Newton Hv shots/s (Born + adjoint)",
+            "value": value, "unit": "shots/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Gaussian random-field model)",
-            "config": {"workload": WORKLOAD if args.n == 192 and args.nt == 2000 else
-                       f"{args.n}^3 nt={args.nt} variant of: " + WORKLOAD,
+            "config": {"workload": desc_w,
                        "grid": list(prob.shape), "nt": prob.nt, "batch_shots": C,
                        "ckpt_k": plan.info("ckpt_k"), "tile": [plan.info("tile_x"),
                                                               plan.info("tile_y"),
@@ -399,7 +455,7 @@ def main():
             "pipeline_roofline": {"bytes_per_step": pipeline_bytes,
                                   "achieved": pipeline_bytes / (t_ms / 1000.0) / 1e9,
                                   "frac": pipeline_bytes / (t_ms / 1000.0) / 1e9 / hbm,
-                                  "model": "44 B/shot + 20 B/batch per cell-step"},
+                                  "model": pipeline_model},
             "e2e": e2e, "plain": plain, "serve": serve, "cpu_baseline": cpu,
             "gpu_launches": launches, "clocks": clk.summary(),
         }

@@ -1,0 +1,76 @@
+"""GPU parity at the benchmark's full grid size (192^3, dx = 0.2 mm, 8x32
+cylinder, seeded random-field model).
+
+The FP64 oracle cannot run the full 256-shot x 2000-step workload in a test,
+so parity against it uses a 2-shot subset and a shortened time axis on the
+full grid; the full time axis is covered by size-independent properties
+(batched shots bit-identical to one shot per launch, reciprocity of the
+point-to-point traces).
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+from golden_util import rel_l2
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def prob():
+    assert torch.cuda.is_available()
+    from openusct_gb300 import build, problems
+    build.build()
+    return problems.cylinder3d(seed=0)
+
+
+def _sub(p, nt):
+    return p.wavelet[:nt]
+
+
+def test_fullsize_traces_and_gradient_vs_fp64(prob):
+    import openusct_gb300.backend as gb
+    nt = 240
+    wav = _sub(prob, nt)
+    sl = [0, 40]
+    d64 = oracle.forward_fmc(prob.m_true, prob.geom, wav, prob.dt, prob.h, nt, None, sl)
+    d32 = gb.forward_fmc(prob.m_true, prob.geom, wav, prob.dt, prob.h, nt, None, sl)
+    assert rel_l2(d32, d64) < 1e-5
+    J64, g64 = oracle.misfit_and_gradient(prob.m0, prob.geom, wav, prob.dt, prob.h, nt, d64, None,
+                                          sl, k=24)
+    J32, g32 = gb.misfit_and_gradient(prob.m0, prob.geom, wav, prob.dt, prob.h, nt, d64,
+                                      src_list=sl, ckpt_k=24)
+    assert abs(J32 - J64) <= 1e-4 * J64
+    assert rel_l2(g32, g64) < 1e-4
+    # 8 seeded directions: GPU gradient . dm against a central difference of the FP64 misfit
+    rng = np.random.default_rng(8)
+    for _ in range(8):
+        dm = rng.standard_normal(prob.m0.shape).astype(np.float64)
+        dm[:5] = dm[-5:] = dm[:, :5] = dm[:, -5:] = dm[:, :, :5] = dm[:, :, -5:] = 0.0
+        dm *= float(np.mean(prob.m0))
+        eps = 1e-6
+        Jp = oracle.misfit(prob.m0 + eps * dm, prob.geom, wav, prob.dt, prob.h, nt, d64,
+                           src_list=sl)
+        Jm = oracle.misfit(prob.m0 - eps * dm, prob.geom, wav, prob.dt, prob.h, nt, d64,
+                           src_list=sl)
+        fd = (Jp - Jm) / (2 * eps)
+        assert abs(float(np.sum(g32 * dm)) - fd) <= 1e-4 * abs(fd)
+
+
+def test_fullsize_batched_equals_one_shot_and_reciprocity(prob):
+    import openusct_gb300.backend as gb
+    sl = [0, 37, 101, 200]
+    m = torch.from_numpy(prob.m_true).cuda()
+    d4 = gb.forward_fmc(m, prob.geom, prob.wavelet, prob.dt, prob.h, prob.nt, None, sl,
+                        batch=4).cpu().numpy()
+    d1 = gb.forward_fmc(m, prob.geom, prob.wavelet, prob.dt, prob.h, prob.nt, None, sl,
+                        batch=1).cpu().numpy()
+    assert np.array_equal(d4, d1)
+    # reciprocity of point-to-point traces (the scheme is symmetric in space)
+    for a in range(len(sl)):
+        for b in range(a + 1, len(sl)):
+            tab = d4[a, :, sl[b]]
+            tba = d4[b, :, sl[a]]
+            assert rel_l2(tab, tba) < 1e-4
