@@ -264,6 +264,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    # a non-default stream: batch sweeps of launch-bound sizes run as CUDA graphs
+    torch.cuda.set_stream(torch.cuda.Stream(device=dev))
 
     from openusct_gb300 import _lib, backend
     from openusct_gb300.geometry import element_csr
@@ -394,6 +396,13 @@ def main():
         torch.cuda.empty_cache()
         tx1, rx1 = element_csr(prob.geom, prob.shape, [0], None)
         pplan = backend.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx1, rx1, batch=1)
+        need = pplan.plain_bytes(True)
+        free = torch.cuda.mem_get_info(dev)[0]
+    if rank == 0 and not args.no_plain and mode == "grad" and need > 0.95 * free:
+        plain = {"value": None, "unit": "shots/s",
+                 "infeasible": f"the plain form keeps the full FP32 history: {need / 2**30:.0f} GiB "
+                               f"> {free / 2**30:.0f} GiB free HBM"}
+    elif rank == 0 and not args.no_plain and mode == "grad":
         pws = torch.empty(pplan.plain_bytes(True), dtype=torch.uint8, device=dev)
         J1 = torch.zeros(1, dtype=torch.float64, device=dev)
         d1 = dobs[0:1].contiguous()
