@@ -145,6 +145,16 @@ int usct_batch_forward(usct_plan* plan, const void* model_ws, void* batch_ws, in
 int usct_batch_misfit(usct_plan* plan, void* batch_ws, int b, const float* dobs, double* J,
                       void* stream);
 
+/*
+ * Misfit of batch b with a selectable misfit: misfit_type 0 = L2 (as
+ * usct_batch_misfit), 1 = global correlation norm, J = sum_j (1 - c_j) with
+ * c_j the normalised zero-lag correlation of trace j and its adjoint source
+ * -(dobs/|dobs| - c dsyn/|dsyn|)/|dsyn| (libuap.hpp:133-162, fwi.py:158-167;
+ * norms and correlations summed in FP64).
+ */
+int usct_batch_misfit_mt(usct_plan* plan, void* batch_ws, int b, const float* dobs,
+                         int misfit_type, double* J, void* stream);
+
 /* Use an arbitrary adjoint source for batch b (device FP32 [n_tx][nt][n_rx]),
  * e.g. dL/d(traces) from an autograd graph. */
 int usct_batch_adjoint_source(usct_plan* plan, void* batch_ws, int b, const float* adj,
@@ -173,6 +183,12 @@ int usct_forward_fmc_dev(usct_plan* plan, const double* m, const double* sponge,
 int usct_misfit_and_gradient_dev(usct_plan* plan, const double* m, const double* sponge,
                                  const double* wavelet, const float* dobs, double* J,
                                  double* grad, void* model_ws, void* batch_ws, void* stream);
+/* misfit_and_gradient with misfit_type 0 (L2) or 1 (GCN), as uap::misfit_and_gradient's
+ * misfit_type argument (libuap.hpp:169-173). */
+int usct_misfit_and_gradient_mt_dev(usct_plan* plan, const double* m, const double* sponge,
+                                    const double* wavelet, const float* dobs, int misfit_type,
+                                    double* J, double* grad, void* model_ws, void* batch_ws,
+                                    void* stream);
 /* fwi.gn_hessian_vector: hv device FP64 dims-shaped; born (NULL = skip) FP32
  * [n_tx][nt][n_rx] receives J v. */
 int usct_gn_hessian_vector_dev(usct_plan* plan, const double* m, const double* sponge,

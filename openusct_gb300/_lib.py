@@ -51,11 +51,14 @@ SIGNATURES = {
     "usct_model_prepare": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "usct_batch_forward": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
     "usct_batch_misfit": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),
+    "usct_batch_misfit_mt": (_i, [_vp, _vp, _i, _vp, _i, _vp, _vp]),
     "usct_batch_adjoint_source": (_i, [_vp, _vp, _i, _vp, _vp]),
     "usct_batch_backward": (_i, [_vp, _vp, _vp, _i, _vp]),
     "usct_model_gradient": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "usct_forward_fmc_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "usct_misfit_and_gradient_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "usct_misfit_and_gradient_mt_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp,
+                                             _vp]),
     "usct_gn_hessian_vector_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "usct_plain_bytes": (ctypes.c_size_t, [_vp, _i]),
     "usct_plain_forward_fmc_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),

@@ -11,9 +11,10 @@ Signatures follow ``simulation/ringfwi/fwi.py`` (forward_fmc :102, misfit :246,
 misfit_and_gradient :266, gn_hessian_vector :410), which is the superset of the
 reference's C++ (software/python/uap.py:34-67) and CuPy
 (software/python/uap_gpu.py:166-233) backends; inputs are NumPy arrays (or CUDA
-tensors), outputs are FP64 NumPy arrays like the reference's.  Error behaviour
-follows the reference GPU backend: a non-L2 misfit raises NotImplementedError
-(uap_gpu.py:191-192), an unknown one ValueError (fwi.py:243).
+tensors), outputs are FP64 NumPy arrays like the reference's.  The misfits are
+those of the reference C++ core, ``l2`` and ``gcn`` (uap.py:41); the Python-only
+robust misfits raise NotImplementedError as the reference GPU backend does for
+non-L2 (uap_gpu.py:191-192), an unknown one ValueError (fwi.py:243).
 
 Everything runs on the CUDA kernels of ``libusct_gb300.so``; a missing library
 or device raises instead of falling back to the CPU.
@@ -179,7 +180,8 @@ def batch_bytes_estimate(shape, nt, n_rx, nslot, C, ckpt_k, mode):
     k = ckpt_k if ckpt_k else max(2, int(round((2.0 * (nt - 1)) ** 0.5)))
     k = min(k, max(2, nt - 1))
     nseg = (nt - 1 + k - 1) // k
-    b = 2 * lv + al(nt * nslot * C * 4) + al(nt * n_rx * C * 4) + al(64 * C * 8)
+    b = (2 * lv + al(nt * nslot * C * 4) + al(nt * n_rx * C * 4) + al(64 * C * 8) +
+         al(n_rx * C * 8))
     if mode >= _lib.MODE_GRADIENT:
         b += (2 + 2 * nseg + k) * lv
     if mode == _lib.MODE_BORN:
@@ -248,13 +250,18 @@ def _out(x, like):
     return x.detach().cpu().numpy().astype(np.float64)
 
 
+_MISFIT_CODES = {"l2": 0, "gcn": 1}
+
+
 def _check_misfit(misfit_type, time_weights):
+    """Returns the engine's code for misfit_type (l2 = 0, gcn = 1, as uap.py:41)."""
     if misfit_type not in _KNOWN_MISFITS:
         raise ValueError(f"unknown misfit_type {misfit_type!r}")
-    if misfit_type != "l2":
-        raise NotImplementedError("the GB300 backend implements the L2 misfit only")
+    if misfit_type not in _MISFIT_CODES:
+        raise NotImplementedError("the GB300 backend implements the l2 and gcn misfits")
     if time_weights is not None:
         raise NotImplementedError("time_weights are not supported by the GB300 backend")
+    return _MISFIT_CODES[misfit_type]
 
 
 # ---------------------------------------------------------------------------
@@ -284,8 +291,8 @@ def forward_fmc(m, geom, wavelet, dt, h, nt, sponge=None, src_list=None, footpri
 def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None,
                         misfit_type="l2", footprints=None, time_weights=None, *, batch=None,
                         ckpt_k=None, tile=None, return_per_shot=False):
-    """L2 waveform misfit and its exact discrete-adjoint gradient in m (FP64)."""
-    _check_misfit(misfit_type, time_weights)
+    """Waveform misfit (l2 or gcn) and its exact discrete-adjoint gradient in m (FP64)."""
+    mt = _check_misfit(misfit_type, time_weights)
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_GRADIENT, batch, ckpt_k,
                   tile)
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -301,8 +308,8 @@ def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list
     mws = plan.workspace("model", plan.model_bytes(), dev)
     bws = plan.workspace(_lib.MODE_GRADIENT, plan.batch_bytes(_lib.MODE_GRADIENT), dev)
     with _on_exec_stream() as st:
-        _lib.check(plan._lib.usct_misfit_and_gradient_dev(
-            plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(od), _ptr(J), _ptr(g), _ptr(mws),
+        _lib.check(plan._lib.usct_misfit_and_gradient_mt_dev(
+            plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(od), mt, _ptr(J), _ptr(g), _ptr(mws),
             _ptr(bws), _stream(st)))
         plan.check(st)
     Jh = J.cpu().numpy()
@@ -314,8 +321,8 @@ def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list
 
 def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, misfit_type="l2",
            footprints=None, time_weights=None, *, batch=None, tile=None):
-    """L2 waveform misfit only (one forward sweep per batch)."""
-    _check_misfit(misfit_type, time_weights)
+    """Waveform misfit (l2 or gcn) only: one forward sweep per batch."""
+    mt = _check_misfit(misfit_type, time_weights)
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_FORWARD, batch, None, tile)
     dev = torch.device("cuda", torch.cuda.current_device())
     md = _to_dev(m, torch.float64, dev)
@@ -335,7 +342,8 @@ def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, misfit
         for b in range(plan.nbatch):
             _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
                                               _lib.MODE_FORWARD, None, s))
-            _lib.check(lib.usct_batch_misfit(plan.handle, _ptr(bws), b, _ptr(od), _ptr(J), s))
+            _lib.check(lib.usct_batch_misfit_mt(plan.handle, _ptr(bws), b, _ptr(od), mt, _ptr(J),
+                                                s))
         plan.check(st)
     return float(np.sum(J.cpu().numpy()))
 

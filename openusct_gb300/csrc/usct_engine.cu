@@ -397,7 +397,8 @@ extern "C" size_t usct_model_bytes(const usct_plan* p) {
 }
 
 struct BatchWS {
-    float* P[2]; float* rs; float* res; double* jpart; float* ck; float* stash; float* L[2]; float* D[2];
+    float* P[2]; float* rs; float* res; double* jpart; double* gj; float* ck; float* stash; float* L[2];
+    float* D[2];
 };
 
 static BatchWS carve_batch(const usct_plan* p, void* base, int mode) {
@@ -409,6 +410,7 @@ static BatchWS carve_batch(const usct_plan* p, void* base, int mode) {
     w.rs = (float*)c; c += al256((size_t)p->nt * p->nslot * p->C * sizeof(float));
     w.res = (float*)c; c += al256((size_t)p->nt * p->n_rx * p->C * sizeof(float));
     w.jpart = (double*)c; c += al256((size_t)JBLK * p->C * sizeof(double));
+    w.gj = (double*)c; c += al256((size_t)p->n_rx * p->C * sizeof(double));
     if (mode >= USCT_MODE_GRADIENT) {
         w.L[0] = (float*)c; c += lv;
         w.L[1] = (float*)c; c += lv;
@@ -427,7 +429,8 @@ extern "C" size_t usct_batch_bytes(const usct_plan* p, int mode) {
     const size_t lv = al256(p->LV * sizeof(float));
     size_t b = 2 * lv + al256((size_t)p->nt * p->nslot * p->C * sizeof(float)) +
                al256((size_t)p->nt * p->n_rx * p->C * sizeof(float)) +
-               al256((size_t)JBLK * p->C * sizeof(double));
+               al256((size_t)JBLK * p->C * sizeof(double)) +
+               al256((size_t)p->n_rx * p->C * sizeof(double));
     if (mode >= USCT_MODE_GRADIENT) b += (2 + 2 * (size_t)p->nseg + (size_t)p->k) * lv;
     if (mode == USCT_MODE_BORN) b += 2 * lv;
     return b;
@@ -536,6 +539,55 @@ __global__ void k_adjsrc(const float* __restrict__ adj, float* res, int C, int n
         const long long r = i / C;
         const int n = (int)(r / nrx), j = (int)(r % nrx);
         res[i] = c < nb ? adj[((long long)(shot0 + c) * nt + n) * nrx + j] : 0.f;
+    }
+}
+
+// GCN adjoint source (libuap.hpp:133-162, fwi.py:158-167) from the traces in
+// res ([nt][n_rx][C]), in place: per (receiver j, shot c) FP64 sums over time
+// of the FP32 traces; gj[j][c] = 1 - c_j for the per-shot misfit.
+__global__ void k_gcn(float* res, const float* __restrict__ dobs, int C, int logC, int nt, int nrx,
+                      int shot0, int nb, double* gj) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nrx * C) return;
+    const int j = idx >> logC, c = idx & (C - 1);
+    float* col = res + (long long)j * C + c;
+    const long long rstride = (long long)nrx * C;
+    if (c >= nb) {
+        for (int n = 0; n < nt; ++n) col[n * rstride] = 0.f;
+        gj[idx] = 0.0;
+        return;
+    }
+    const float* ob = dobs + (long long)(shot0 + c) * nt * nrx + j;
+    const double eps = 1e-12;
+    double sn = 0.0, on = 0.0;
+    for (int n = 0; n < nt; ++n) {
+        const double sv = (double)col[n * rstride];
+        const double ov = (double)ob[(long long)n * nrx];
+        sn += sv * sv;
+        on += ov * ov;
+    }
+    sn = sqrt(sn) + eps;
+    on = sqrt(on) + eps;
+    double cc = 0.0;
+    for (int n = 0; n < nt; ++n) {
+        const double sv = (double)col[n * rstride];
+        const double ov = (double)ob[(long long)n * nrx];
+        cc += (sv / sn) * (ov / on);
+    }
+    for (int n = 0; n < nt; ++n) {
+        const double sv = (double)col[n * rstride];
+        const double ov = (double)ob[(long long)n * nrx];
+        col[n * rstride] = (float)(-(ov / on - cc * (sv / sn)) / sn);
+    }
+    gj[idx] = 1.0 - cc;
+}
+
+__global__ void k_gcn_j(const double* __restrict__ gj, int C, int nrx, int shot0, int nb, double* J) {
+    const int c = threadIdx.x;
+    if (c < nb) {
+        double s = 0.0;
+        for (int j = 0; j < nrx; ++j) s += gj[(long long)j * C + c];
+        J[shot0 + c] = s;
     }
 }
 
@@ -999,6 +1051,28 @@ extern "C" int usct_batch_misfit(usct_plan* p, void* batch_ws, int b, const floa
     return USCT_OK;
 }
 
+extern "C" int usct_batch_misfit_mt(usct_plan* p, void* batch_ws, int b, const float* dobs,
+                                    int misfit_type, double* J, void* stream) {
+    if (misfit_type == 0) return usct_batch_misfit(p, batch_ws, b, dobs, J, stream);
+    if (misfit_type != 1) return set_err(USCT_ERR_ARG, "misfit_type must be 0 (L2) or 1 (GCN)");
+    if (!p || !batch_ws || !dobs) return set_err(USCT_ERR_ARG, "null argument");
+    if (b < 0 || b >= p->nbatch) return set_err(USCT_ERR_ARG, "batch %d out of range", b);
+    cudaStream_t s = (cudaStream_t)stream;
+    const BatchWS B = carve_batch(p, batch_ws, USCT_MODE_FORWARD);
+    TRY(gather(p, B, b, nullptr, nullptr, 2, s));   // res = traces
+    const int shot0 = b * p->C;
+    const int nb = std::min(p->C, p->n_tx - shot0);
+    const int n = p->n_rx * p->C;
+    k_gcn<<<(n + 127) / 128, 128, 0, s>>>(B.res, dobs, p->C, p->logC, p->nt, p->n_rx, shot0, nb, B.gj);
+    ++p->launches;
+    if (J) {
+        k_gcn_j<<<1, 64, 0, s>>>(B.gj, p->C, p->n_rx, shot0, nb, J);
+        ++p->launches;
+    }
+    CUDA_TRY(cudaGetLastError());
+    return USCT_OK;
+}
+
 extern "C" int usct_batch_adjoint_source(usct_plan* p, void* batch_ws, int b, const float* adj,
                                          void* stream) {
     if (!p || !batch_ws || !adj) return set_err(USCT_ERR_ARG, "null argument");
@@ -1095,6 +1169,21 @@ extern "C" int usct_misfit_and_gradient_dev(usct_plan* p, const double* m, const
     for (int b = 0; b < p->nbatch; ++b) {
         TRY(usct_batch_forward(p, model_ws, batch_ws, b, USCT_MODE_GRADIENT, nullptr, stream));
         TRY(usct_batch_misfit(p, batch_ws, b, dobs, J, stream));
+        TRY(usct_batch_backward(p, model_ws, batch_ws, b, stream));
+    }
+    return usct_model_gradient(p, model_ws, m, grad, stream);
+}
+
+extern "C" int usct_misfit_and_gradient_mt_dev(usct_plan* p, const double* m, const double* sponge,
+                                               const double* wavelet, const float* dobs,
+                                               int misfit_type, double* J, double* grad,
+                                               void* model_ws, void* batch_ws, void* stream) {
+    if (misfit_type != 0 && misfit_type != 1)
+        return set_err(USCT_ERR_ARG, "misfit_type must be 0 (L2) or 1 (GCN)");
+    TRY(usct_model_prepare(p, model_ws, m, sponge, nullptr, wavelet, stream));
+    for (int b = 0; b < p->nbatch; ++b) {
+        TRY(usct_batch_forward(p, model_ws, batch_ws, b, USCT_MODE_GRADIENT, nullptr, stream));
+        TRY(usct_batch_misfit_mt(p, batch_ws, b, dobs, misfit_type, J, stream));
         TRY(usct_batch_backward(p, model_ws, batch_ws, b, stream));
     }
     return usct_model_gradient(p, model_ws, m, grad, stream);

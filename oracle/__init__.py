@@ -53,6 +53,7 @@ def _load():
                 build()
             lib = ctypes.CDLL(_LIB)
             lib.usct_oracle_misfit_and_gradient.restype = ctypes.c_double
+            lib.usct_oracle_misfit_and_gradient_mt.restype = ctypes.c_double
             _lib = lib
     return _lib
 
@@ -133,28 +134,39 @@ def forward_fmc(m, geom, wavelet, dt, h, nt, sponge=None, src_list=None, footpri
     return data
 
 
+_MT = {"l2": 0, "gcn": 1}
+
+
 def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None,
-                        footprints=None, k=0):
-    """FP64 restatement of fwi.misfit_and_gradient (L2).  k = 0: full history
-    (the reference's memory plan); k > 0: checkpoints every k steps."""
+                        footprints=None, k=0, misfit_type="l2"):
+    """FP64 restatement of fwi.misfit_and_gradient (L2 or GCN).  k = 0: full
+    history (the reference's memory plan); k > 0: checkpoints every k steps."""
     lib = _load()
     m, dims, wav, sp = _common(m, wavelet, sponge)
     (tp, ti, tw), (rp, ri, rw), ntx, nrx = _geometry(geom, m.shape, src_list, footprints)
     dobs = np.ascontiguousarray(dobs, np.float64)
     g = np.zeros(m.shape)
-    J = lib.usct_oracle_misfit_and_gradient(
+    J = lib.usct_oracle_misfit_and_gradient_mt(
         _p(m, _dp), _p(dims, _ip), m.ndim, ctypes.c_double(h), ctypes.c_double(dt), int(nt),
         ntx, _p(tp, _ip), _p(ti, _lp), _p(tw, _dp), nrx, _p(rp, _ip), _p(ri, _lp), _p(rw, _dp),
-        _p(wav, _dp), None if sp is None else _p(sp, _dp), _p(dobs, _dp), _p(g, _dp), int(k))
+        _p(wav, _dp), None if sp is None else _p(sp, _dp), _p(dobs, _dp), _p(g, _dp), int(k),
+        _MT[misfit_type])
     return float(J), g
 
 
-def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, footprints=None):
+def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, footprints=None,
+           misfit_type="l2"):
     d = forward_fmc(m, geom, wavelet, dt, h, nt, sponge, src_list, footprints)
     J = 0.0
     for i in range(d.shape[0]):
-        r = d[i] - dobs[i]
-        J += 0.5 * float(np.sum(r * r))
+        if misfit_type == "gcn":   # libuap.hpp:133-154
+            eps = 1e-12
+            ns = np.sqrt(np.sum(d[i] * d[i], axis=0)) + eps
+            no = np.sqrt(np.sum(dobs[i] * dobs[i], axis=0)) + eps
+            J += float(np.sum(1.0 - np.sum((d[i] / ns) * (dobs[i] / no), axis=0)))
+        else:
+            r = d[i] - dobs[i]
+            J += 0.5 * float(np.sum(r * r))
     return J
 
 
@@ -206,7 +218,7 @@ def forward_fmc32(m, geom, wavelet, dt, h, nt, sponge=None, src_list=None, footp
 
 
 def misfit_and_gradient32(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None,
-                          footprints=None, C=1):
+                          footprints=None, C=1, misfit_type="l2"):
     """Returns (J per transmit float64 array, g float64) in kernel order for a
     batch width of C shot channels."""
     lib = _load()
@@ -215,11 +227,11 @@ def misfit_and_gradient32(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_li
     dobs = np.ascontiguousarray(dobs, np.float64)
     g = np.zeros(m.shape)
     J = np.zeros(ntx)
-    rc = lib.usct_oracle32_misfit_and_gradient(
+    rc = lib.usct_oracle32_misfit_and_gradient_mt(
         _p(m, _dp), _p(dims, _ip), m.ndim, ctypes.c_double(h), ctypes.c_double(dt), int(nt),
         ntx, _p(tp, _ip), _p(ti, _lp), _p(tw, _dp), nrx, _p(rp, _ip), _p(ri, _lp), _p(rw, _dp),
         _p(wav, _dp), None if sp is None else _p(sp, _dp), _p(dobs, _dp), int(C), _p(J, _dp),
-        _p(g, _dp))
+        _p(g, _dp), _MT[misfit_type])
     if rc != 0:
         raise ValueError("C must be a power of two <= 64")
     return J, g
@@ -260,7 +272,7 @@ def ref_forward_fmc(m, geom, wavelet, dt, h, nt, src_list=None):
     return data
 
 
-def ref_misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, src_list=None):
+def ref_misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, src_list=None, misfit_type="l2"):
     lib = _load_ref()
     m = np.ascontiguousarray(m, np.float64)
     dims = np.asarray(m.shape, np.int32)
@@ -273,5 +285,5 @@ def ref_misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, src_list=None):
     J = lib.usct_ref_misfit_and_gradient(_p(m, _dp), _p(dims, _ip), m.ndim, ctypes.c_double(h),
                                          ctypes.c_double(dt), int(nt), _p(tx, _ip), len(tx),
                                          _p(rec, _ip), len(rec), _p(wav, _dp), _p(dobs, _dp),
-                                         _p(g, _dp), 0)
+                                         _p(g, _dp), _MT[misfit_type])
     return float(J), g

@@ -162,6 +162,43 @@ static double residual64(const double* dsyn, const double* dobs, size_t total, d
     return J;
 }
 
+/* GCN adjoint source (libuap.hpp:133-162, fwi.py:158-167): per receiver trace
+ * ns = |dsyn|+eps, no = |dobs|+eps, c = <dsyn/ns, dobs/no>, J = sum (1 - c),
+ * res = -(dobs/no - c dsyn/ns)/ns. */
+static double residual64_gcn(const double* dsyn, const double* dobs, int nt, int nrx, double* res) {
+    const double eps = 1e-12;
+    double* ns = (double*)calloc((size_t)nrx, sizeof(double));
+    double* no = (double*)calloc((size_t)nrx, sizeof(double));
+    double* c = (double*)calloc((size_t)nrx, sizeof(double));
+    for (int k = 0; k < nt; ++k) {
+        const double* srow = dsyn + (size_t)k * nrx;
+        const double* orow = dobs + (size_t)k * nrx;
+        for (int j = 0; j < nrx; ++j) {
+            ns[j] += srow[j] * srow[j];
+            no[j] += orow[j] * orow[j];
+        }
+    }
+    for (int j = 0; j < nrx; ++j) {
+        ns[j] = sqrt(ns[j]) + eps;
+        no[j] = sqrt(no[j]) + eps;
+    }
+    for (int k = 0; k < nt; ++k) {
+        const double* srow = dsyn + (size_t)k * nrx;
+        const double* orow = dobs + (size_t)k * nrx;
+        for (int j = 0; j < nrx; ++j) c[j] += (srow[j] / ns[j]) * (orow[j] / no[j]);
+    }
+    double J = 0.0;
+    for (int j = 0; j < nrx; ++j) J += 1.0 - c[j];
+    for (int k = 0; k < nt; ++k) {
+        const double* srow = dsyn + (size_t)k * nrx;
+        const double* orow = dobs + (size_t)k * nrx;
+        double* rrow = res + (size_t)k * nrx;
+        for (int j = 0; j < nrx; ++j) rrow[j] = -(orow[j] / no[j] - c[j] * (srow[j] / ns[j])) / ns[j];
+    }
+    free(ns); free(no); free(c);
+    return J;
+}
+
 /* Backward sweep for one transmit (libuap.hpp:196-219, fwi.py:306-326):
  *   lam^k = 2 lam^{k+1} - lam^{k+2} + L(S lam^{k+1});  lam^k *= sponge;
  *   lam^k[rx] -= r^k * w;  g += lam^k * (U^k - 2U^{k-1} + U^{k-2}).
@@ -260,11 +297,30 @@ int usct_oracle_forward_fmc(const double* m, const int* dims, int ndim, double h
 /* misfit_and_gradient (L2).  kck == 0: full history per transmit, exactly the
  * reference's memory plan; kck > 0: checkpoints every kck steps.  grad gets
  * sum_t g_t / m; returns J. */
+double usct_oracle_misfit_and_gradient_mt(const double* m, const int* dims, int ndim, double h,
+                                          double dt, int nt, int n_tx, const int* tx_ptr,
+                                          const i64* tx_idx, const double* tx_w, int nrx,
+                                          const int* rx_ptr, const i64* rx_idx, const double* rx_w,
+                                          const double* wav, const double* sponge, const double* dobs,
+                                          double* grad, int kck, int misfit_type);
+
 double usct_oracle_misfit_and_gradient(const double* m, const int* dims, int ndim, double h, double dt,
                                        int nt, int n_tx, const int* tx_ptr, const i64* tx_idx,
                                        const double* tx_w, int nrx, const int* rx_ptr,
                                        const i64* rx_idx, const double* rx_w, const double* wav,
                                        const double* sponge, const double* dobs, double* grad, int kck) {
+    return usct_oracle_misfit_and_gradient_mt(m, dims, ndim, h, dt, nt, n_tx, tx_ptr, tx_idx, tx_w,
+                                              nrx, rx_ptr, rx_idx, rx_w, wav, sponge, dobs, grad,
+                                              kck, 0);
+}
+
+/* misfit_type 0 = L2, 1 = GCN (libuap.hpp:169, misfit_type). */
+double usct_oracle_misfit_and_gradient_mt(const double* m, const int* dims, int ndim, double h,
+                                          double dt, int nt, int n_tx, const int* tx_ptr,
+                                          const i64* tx_idx, const double* tx_w, int nrx,
+                                          const int* rx_ptr, const i64* rx_idx, const double* rx_w,
+                                          const double* wav, const double* sponge, const double* dobs,
+                                          double* grad, int kck, int misfit_type) {
     G64 g; double* S;
     setup64(&g, m, dims, ndim, h, dt, nt, wav, sponge, nrx, rx_ptr, rx_idx, rx_w, &S);
     const size_t N = g.N;
@@ -277,7 +333,10 @@ double usct_oracle_misfit_and_gradient(const double* m, const int* dims, int ndi
     for (int t = 0; t < n_tx; ++t) {
         const int ns = tx_ptr[t + 1] - tx_ptr[t];
         forward64(&g, ns, tx_idx + tx_ptr[t], tx_w + tx_ptr[t], dsyn, hist, kck, ck);
-        J += residual64(dsyn, dobs + (size_t)t * nt * nrx, (size_t)nt * nrx, res);
+        if (misfit_type == 1)
+            J += residual64_gcn(dsyn, dobs + (size_t)t * nt * nrx, nt, nrx, res);
+        else
+            J += residual64(dsyn, dobs + (size_t)t * nt * nrx, (size_t)nt * nrx, res);
         backward64(&g, ns, tx_idx + tx_ptr[t], tx_w + tx_ptr[t], res, hist, kck, ck, grad);
     }
     for (size_t i = 0; i < N; ++i) grad[i] /= m[i];
@@ -548,7 +607,8 @@ static int grad32_impl(const double* m, const int* dims, int ndim, double h, dou
                        int n_tx, const int* tx_ptr, const i64* tx_idx, const double* tx_w,
                        int nrx, const int* rx_ptr, const i64* rx_idx, const double* rx_w,
                        const double* wav, const double* sponge, const double* dobs, int C,
-                       double* J_out, double* grad, const double* born_v, float* born_out) {
+                       double* J_out, double* grad, const double* born_v, float* born_out,
+                       int misfit_type) {
     G32 g;
     setup32(&g, m, dims, ndim, h, dt, nt, wav, sponge, nrx, rx_ptr, rx_idx, rx_w);
     const size_t N = g.N;
@@ -631,7 +691,36 @@ static int grad32_impl(const double* m, const int* dims, int ndim, double h, dou
                 }
             }
             /* adjoint source */
-            if (!born_v) {
+            if (!born_v && misfit_type == 1) {
+                /* GCN as the device computes it: per receiver, FP64 sums over time of
+                 * the FP32 traces (sequential in n), J = sum_j (1 - c_j) in j order */
+                const double* ob = dobs + (size_t)t * nt * nrx;
+                const double eps = 1e-12;
+                double J = 0.0;
+                for (int j = 0; j < nrx; ++j) {
+                    double sn = 0.0, on = 0.0, cc = 0.0;
+                    for (int n = 0; n < nt; ++n) {
+                        const double sv = (double)dsyn[(size_t)n * nrx + j];
+                        const double ov = (double)(float)ob[(size_t)n * nrx + j];
+                        sn += sv * sv;
+                        on += ov * ov;
+                    }
+                    sn = sqrt(sn) + eps;
+                    on = sqrt(on) + eps;
+                    for (int n = 0; n < nt; ++n) {
+                        const double sv = (double)dsyn[(size_t)n * nrx + j];
+                        const double ov = (double)(float)ob[(size_t)n * nrx + j];
+                        cc += (sv / sn) * (ov / on);
+                    }
+                    for (int n = 0; n < nt; ++n) {
+                        const double sv = (double)dsyn[(size_t)n * nrx + j];
+                        const double ov = (double)(float)ob[(size_t)n * nrx + j];
+                        res[c][(size_t)n * nrx + j] = (float)(-(ov / on - cc * (sv / sn)) / sn);
+                    }
+                    J += 1.0 - cc;
+                }
+                if (J_out) J_out[t] = J;
+            } else if (!born_v) {
                 const double* ob = dobs + (size_t)t * nt * nrx;
                 double J = 0.0;
                 for (size_t z = 0; z < (size_t)nt * nrx; ++z) {
@@ -699,7 +788,18 @@ int usct_oracle32_misfit_and_gradient(const double* m, const int* dims, int ndim
                                       double* J_out, double* grad) {
     if (C < 1 || C > 64 || (C & (C - 1))) return -1;
     return grad32_impl(m, dims, ndim, h, dt, nt, n_tx, tx_ptr, tx_idx, tx_w, nrx, rx_ptr, rx_idx,
-                       rx_w, wav, sponge, dobs, C, J_out, grad, NULL, NULL);
+                       rx_w, wav, sponge, dobs, C, J_out, grad, NULL, NULL, 0);
+}
+
+int usct_oracle32_misfit_and_gradient_mt(const double* m, const int* dims, int ndim, double h,
+                                         double dt, int nt, int n_tx, const int* tx_ptr,
+                                         const i64* tx_idx, const double* tx_w, int nrx,
+                                         const int* rx_ptr, const i64* rx_idx, const double* rx_w,
+                                         const double* wav, const double* sponge, const double* dobs,
+                                         int C, double* J_out, double* grad, int misfit_type) {
+    if (C < 1 || C > 64 || (C & (C - 1))) return -1;
+    return grad32_impl(m, dims, ndim, h, dt, nt, n_tx, tx_ptr, tx_idx, tx_w, nrx, rx_ptr, rx_idx,
+                       rx_w, wav, sponge, dobs, C, J_out, grad, NULL, NULL, misfit_type);
 }
 
 int usct_oracle32_gn_hessian_vector(const double* m, const int* dims, int ndim, double h, double dt, int nt,
@@ -709,5 +809,5 @@ int usct_oracle32_gn_hessian_vector(const double* m, const int* dims, int ndim, 
                                     double* out, float* born_out) {
     if (C < 1 || C > 64 || (C & (C - 1))) return -1;
     return grad32_impl(m, dims, ndim, h, dt, nt, n_tx, tx_ptr, tx_idx, tx_w, nrx, rx_ptr, rx_idx,
-                       rx_w, wav, sponge, NULL, C, NULL, out, v, born_out);
+                       rx_w, wav, sponge, NULL, C, NULL, out, v, born_out, 0);
 }

@@ -25,8 +25,9 @@ own tests:
                      FP32-GPU-vs-FP64 parity problem, every third element)
 
 Each fixture stores the inputs (m, m0, element indices, footprints as CSR,
-wavelet, dt, h, nt, src_list, sponge) and the reference outputs (dobs, J, g,
-and Hv for the Gauss-Newton cases).
+wavelet, dt, h, nt, src_list, sponge) and the reference outputs (dobs, J, g;
+J_gcn, g_gcn for the GCN misfit on point-element cases; Hv for the
+Gauss-Newton cases).
 """
 
 from __future__ import annotations
@@ -80,11 +81,20 @@ def main():
         out = dict(m_true=m_true, m0=m0, idx=idx, wavelet=wav, dt=dt, h=h, nt=nt,
                    src_list=np.asarray(src_list, np.int32), dobs=dobs, J=J, g=g,
                    sponge=np.zeros(0) if sponge is None else sponge)
+        # the GCN misfit (fwi.py:158-167; libuap.hpp misfit_type=1)
+        Jg, gg = fwi.misfit_and_gradient(m0, geom, wav, dt, h, nt, dobs, sponge, src_list,
+                                         misfit_type="gcn")
+        out["J_gcn"] = Jg
+        out["g_gcn"] = gg
         if with_cpp:
             out["dobs_cpp"] = oracle.ref_forward_fmc(m_true, geom, wav, dt, h, nt, src_list)
             Jc, gc = oracle.ref_misfit_and_gradient(m0, geom, wav, dt, h, nt, dobs, src_list)
             out["J_cpp"] = Jc
             out["g_cpp"] = gc
+            Jgc, ggc = oracle.ref_misfit_and_gradient(m0, geom, wav, dt, h, nt, dobs, src_list,
+                                                      misfit_type="gcn")
+            out["J_gcn_cpp"] = Jgc
+            out["g_gcn_cpp"] = ggc
             assert np.abs(out["dobs_cpp"] - dobs).max() <= 1e-12 * np.abs(dobs).max()
             assert abs(Jc - J) <= 1e-12 * abs(J)
         save(name, **out)

@@ -238,11 +238,39 @@ def test_directional_derivatives_eight_seeded_directions():
         assert abs(float(np.sum(g * dm)) - fd) <= 1e-4 * abs(fd)
 
 
+GCN_CASES = ["ring2d_point", "ring2d_sponge", "cyl3d_point", "odd2d", "odd3d", "parity2d",
+             "parity3d", "gpu3d"]
+
+
+@pytest.mark.parametrize("name", GCN_CASES)
+@pytest.mark.parametrize("C", [1, 4])
+def test_gcn_gradient_bit_exact_and_vs_reference(name, C):
+    """The GCN misfit (libuap.hpp misfit_type=1): GPU == FP32 restatement bit
+    for bit; within tolerance of the reference's FP64 result."""
+    c = load(name)
+    a = c.args()
+    Jr, gr = oracle.misfit_and_gradient32(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt,
+                                          c["dobs"], a["sponge"], a["src_list"], None, C=C,
+                                          misfit_type="gcn")
+    J, g, Js = gb().misfit_and_gradient(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt,
+                                        c["dobs"], a["sponge"], a["src_list"], misfit_type="gcn",
+                                        batch=C, ckpt_k=6, return_per_shot=True)
+    assert np.array_equal(Js, Jr)
+    assert np.array_equal(g, gr)
+    assert abs(J - float(c["J_gcn"])) <= 1e-5 * abs(float(c["J_gcn"]))
+    assert rel_l2(g, c["g_gcn"]) < 1e-4
+    Jm = gb().misfit(c["m_true"] * 1.001, c.geom, a["wavelet"], c.dt, c.h, c.nt, c["dobs"],
+                     a["sponge"], a["src_list"], misfit_type="gcn")
+    Jo = oracle.misfit(c["m_true"] * 1.001, c.geom, a["wavelet"], c.dt, c.h, c.nt, c["dobs"],
+                       a["sponge"], a["src_list"], misfit_type="gcn")
+    assert abs(Jm - Jo) <= 1e-4 * abs(Jo)
+
+
 def test_error_conventions():
     c = load("ring2d_point")
     with pytest.raises(NotImplementedError):
         gb().misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
-                                 src_list=c.src_list, misfit_type="gcn")
+                                 src_list=c.src_list, misfit_type="envelope")
     with pytest.raises(ValueError):
         gb().misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
                                  src_list=c.src_list, misfit_type="nope")

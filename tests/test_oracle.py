@@ -145,3 +145,33 @@ def test_bit_identical_to_reference_cpp_on_fresh_inputs():
     Jr, gr = oracle.ref_misfit_and_gradient(m0, idx, wav, 1e-7, 1e-3, 90, d_ref, [1, 4])
     Jo, go = oracle.misfit_and_gradient(m0, idx, wav, 1e-7, 1e-3, 90, d_ref, None, [1, 4], k=5)
     assert Jr == Jo and np.array_equal(gr, go)
+
+
+GCN_CASES = ["ring2d_point", "ring2d_sponge", "cyl3d_point", "odd2d", "odd3d", "parity2d",
+             "parity3d", "gpu3d"]
+
+
+@pytest.mark.parametrize("name", GCN_CASES)
+def test_gcn_gradient_matches_reference(name):
+    """The GCN misfit (fwi.py:158-167, libuap.hpp:133-162): FP64 restatement
+    against the reference's Python, bit for bit against its C++ core."""
+    c = load(name)
+    a = c.args()
+    J, g = oracle.misfit_and_gradient(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt, c["dobs"],
+                                      a["sponge"], a["src_list"], None, k=9, misfit_type="gcn")
+    assert abs(J - float(c["J_gcn"])) <= 1e-12 * abs(float(c["J_gcn"]))
+    assert rel_max(g, c["g_gcn"]) < 1e-10
+    if "J_gcn_cpp" in c:
+        J0, g0 = oracle.misfit_and_gradient(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt,
+                                            c["dobs"], None, a["src_list"], misfit_type="gcn")
+        assert J0 == float(c["J_gcn_cpp"]) and np.array_equal(g0, c["g_gcn_cpp"])
+
+
+@pytest.mark.parametrize("name", ["ring2d_point", "cyl3d_point", "parity2d"])
+def test_gcn_fp32_restatement_within_tolerance(name):
+    c = load(name)
+    a = c.args()
+    J, g = oracle.misfit_and_gradient32(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt, c["dobs"],
+                                        a["sponge"], a["src_list"], None, C=4, misfit_type="gcn")
+    assert abs(J.sum() - float(c["J_gcn"])) <= 1e-5 * abs(float(c["J_gcn"]))
+    assert rel_l2(g, c["g_gcn"]) < 1e-4
