@@ -73,6 +73,9 @@ extern "C" {
 #define USCT_SET_STAGES_ADJ 2    /* planes in the adjoint TMA ring (3..8) */
 #define USCT_SET_GRAPHS 3        /* 1 = capture each batch sweep as a CUDA graph on first
                                     use (per stream/buffer set) and replay it afterwards */
+#define USCT_SET_WAIT_TEST 4     /* test hook: 1 = the TMA ring's first stage expects bytes
+                                    that never arrive, so its bounded wait gives up and the
+                                    error is reported by usct_plan_check (no fault) */
 
 /* One-line message describing the last error on this thread ("" if none). */
 const char* usct_last_error(void);

@@ -27,7 +27,7 @@ MODE_BORN = 2
 
 INFO = {"batch": 0, "nbatch": 1, "ckpt_k": 2, "nseg": 3, "tile_x": 4, "tile_y": 5,
         "zchunk": 6, "level_floats": 7, "launches": 8, "variant": 9}
-SET = {"variant": 0, "stages": 1, "stages_adj": 2, "graphs": 3}
+SET = {"variant": 0, "stages": 1, "stages_adj": 2, "graphs": 3, "wait_test": 4}
 
 _vp = ctypes.c_void_p
 _i = ctypes.c_int

@@ -107,6 +107,7 @@ struct usct_plan {
     std::unordered_map<uint64_t, CUtensorMap> maps;
     // CUDA graphs of whole batch sweeps, keyed by (op, batch, mode, buffers)
     bool use_graphs = false;
+    int wait_test = 0;   // USCT_SET_WAIT_TEST
     struct Captured {
         cudaGraphExec_t exec;
         long long kernels;
@@ -715,7 +716,9 @@ static void init_tma_attributes() {
     } break;
 
 template <bool BORN>
-static int launch_fwd_tma(usct_plan* p, const FwdArgs& a, cudaStream_t s) {
+static int launch_fwd_tma(usct_plan* p, const FwdArgs& a0, cudaStream_t s) {
+    FwdArgs a = a0;
+    a.wait_test = p->wait_test;
     FwdMaps mp;
     memset(&mp, 0, sizeof(mp));
     TRY(get_map(p, a.pc, MK_WF_HALO, &mp.pc));
@@ -759,7 +762,9 @@ static int launch_fwd_tma(usct_plan* p, const FwdArgs& a, cudaStream_t s) {
         k<<<grid, dim3(TX, TY_), smem, s>>>(a, mp, R, p->d_err);                             \
     } break;
 
-static int launch_adj_tma(usct_plan* p, const AdjArgs& a, cudaStream_t s) {
+static int launch_adj_tma(usct_plan* p, const AdjArgs& a0, cudaStream_t s) {
+    AdjArgs a = a0;
+    a.wait_test = p->wait_test;
     AdjMaps mp;
     memset(&mp, 0, sizeof(mp));
     TRY(get_map(p, a.l1, MK_WF_HALO, &mp.l1));
@@ -866,6 +871,10 @@ extern "C" int usct_plan_set(usct_plan* p, int key, int64_t value) {
         case USCT_SET_GRAPHS:
             p->use_graphs = value != 0;
             if (!p->use_graphs) drop_graphs(p);
+            return USCT_OK;
+        case USCT_SET_WAIT_TEST:
+            p->wait_test = value != 0;
+            drop_graphs(p);
             return USCT_OK;
         default: return set_err(USCT_ERR_ARG, "unknown setting %d", key);
     }

@@ -86,6 +86,7 @@ struct FwdArgs {
     const float* dpp;   // dp^{n-2}
     float* dn;          // dp^n (may alias dpp)
     const float* vm;    // v/m (cell layout)
+    int wait_test;      // test hook: nonzero makes the first ring stage unreachable
 };
 
 struct AdjArgs {
@@ -100,6 +101,7 @@ struct AdjArgs {
     const int* r_ptr;
     const RxEnt* r_ent;
     const float* res;   // adjoint source of step k: [n_rx][C]
+    int wait_test;      // test hook: nonzero makes the first ring stage unreachable
 };
 
 __device__ __forceinline__ float4 f4zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }

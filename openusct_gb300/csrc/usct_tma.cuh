@@ -257,6 +257,7 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         const bool inner = i >= 1 && i <= nloc - 2;
         uint32_t bytes = b_halo * (BORN ? 2u : 1u);
         if (inner) bytes += b_own * (BORN ? 2u : 1u) + b_cell * (1u + (has_sp ? 1u : 0u) + (BORN ? 1u : 0u));
+        if (a.wait_test && i == 0) bytes += 16u;   // never delivered: exercises the bounded wait
         mbar_expect_tx(bar, bytes);
         if (C >= 4) tma4(st, &mp.pc, bar, 0, x0c - 1, y0 - HR, p);
         else tma3(st, &mp.pc, bar, fx0 - 4, y0 - HR, p);
@@ -481,6 +482,7 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
         const bool inner = i >= 1 && i <= nloc - 2;
         uint32_t bytes = b_halo + b_sh;
         if (inner) bytes += 2 * b_own + (has_sp ? b_cell : 0u) + (has_g ? 2 * b_cell : 0u);
+        if (a.wait_test && i == 0) bytes += 16u;   // never delivered: exercises the bounded wait
         mbar_expect_tx(bar, bytes);
         if (C >= 4) tma4(st, &mp.l1, bar, 0, x0c - 1, y0 - HR, p);
         else tma3(st, &mp.l1, bar, fx0 - 4, y0 - HR, p);

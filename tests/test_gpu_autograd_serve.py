@@ -113,3 +113,22 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
         if q.kind == "gradient":
             J, g = gb.misfit_and_gradient(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt, q.dobs)
             assert rel_l2(r.g, g) < 1e-5 and abs(r.J - J) <= 1e-9 * abs(J)
+
+
+def test_bounded_wait_reports_and_recovers():
+    """A TMA stage whose bytes never all arrive: the kernel's bounded wait gives
+    up, the error is reported on the host, later launches skip their work, and
+    the context stays usable for a correct run afterwards."""
+    import openusct_gb300.backend as gb
+    from openusct_gb300._lib import USCTError
+    c = load("cyl3d_point")
+    args = (c["m_true"], c.geom, c.wavelet, c.dt, c.h, c.nt, None, c.src_list)
+    ref = gb.forward_fmc(*args, batch=4, tile=(32, 8, 0, 1))
+    plan = gb._PLANS[next(reversed(gb._PLANS))]
+    assert plan.info("variant") == 1
+    plan.set("wait_test", 1)
+    with pytest.raises(USCTError, match="gave up waiting"):
+        gb.forward_fmc(*args, batch=4, tile=(32, 8, 0, 1))
+    plan.set("wait_test", 0)
+    again = gb.forward_fmc(*args, batch=4, tile=(32, 8, 0, 1))
+    assert np.array_equal(again, ref)
