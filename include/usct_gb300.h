@@ -228,6 +228,12 @@ int usct_forward_fmc(const double* m, const int* dims, int ndim, double h, doubl
 int usct_misfit_and_gradient(const double* m, const int* dims, int ndim, double h, double dt,
                              int nt, const int* tx_lin, int n_tx, const int* rec_lin, int n_rec,
                              const double* wavelet, const double* dobs, double* grad, double* J);
+/* The same with uap::misfit_and_gradient's misfit_type (0 = L2, 1 = GCN), in the
+ * reference's argument position (libuap.hpp:169-173); J is returned through *J. */
+int usct_misfit_and_gradient_mt(const double* m, const int* dims, int ndim, double h, double dt,
+                                int nt, const int* tx_lin, int n_tx, const int* rec_lin,
+                                int n_rec, const double* wavelet, const double* dobs, double* grad,
+                                int misfit_type, double* J);
 
 /* ---- a forward FMC that allocates no device memory ---- */
 /*

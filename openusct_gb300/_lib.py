@@ -66,6 +66,8 @@ SIGNATURES = {
     "usct_forward_fmc": (_i, [_dp, _ip, _i, _d, _d, _i, _ip, _i, _ip, _i, _dp, _dp]),
     "usct_misfit_and_gradient": (_i, [_dp, _ip, _i, _d, _d, _i, _ip, _i, _ip, _i, _dp, _dp, _dp,
                                       _dp]),
+    "usct_misfit_and_gradient_mt": (_i, [_dp, _ip, _i, _d, _d, _i, _ip, _i, _ip, _i, _dp, _dp,
+                                         _dp, _i, _dp]),
     "usct_forward_fmc_noalloc": (_i, [_i, _ip, _d, _d, _i, _i, _ip, _lp, _dp, _i, _ip, _lp, _dp,
                                       _vp, _vp, _vp, _vp, _vp]),
 }

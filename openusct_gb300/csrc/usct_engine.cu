@@ -1259,10 +1259,25 @@ extern "C" int usct_forward_fmc(const double* m, const int* dims, int ndim, doub
     return USCT_OK;
 }
 
+extern "C" int usct_misfit_and_gradient_mt(const double* m, const int* dims, int ndim, double h,
+                                           double dt, int nt, const int* tx_lin, int n_tx,
+                                           const int* rec_lin, int n_rec, const double* wavelet,
+                                           const double* dobs, double* grad, int misfit_type,
+                                           double* J);
+
 extern "C" int usct_misfit_and_gradient(const double* m, const int* dims, int ndim, double h,
                                         double dt, int nt, const int* tx_lin, int n_tx,
                                         const int* rec_lin, int n_rec, const double* wavelet,
                                         const double* dobs, double* grad, double* J) {
+    return usct_misfit_and_gradient_mt(m, dims, ndim, h, dt, nt, tx_lin, n_tx, rec_lin, n_rec,
+                                       wavelet, dobs, grad, 0, J);
+}
+
+extern "C" int usct_misfit_and_gradient_mt(const double* m, const int* dims, int ndim, double h,
+                                           double dt, int nt, const int* tx_lin, int n_tx,
+                                           const int* rec_lin, int n_rec, const double* wavelet,
+                                           const double* dobs, double* grad, int misfit_type,
+                                           double* J) {
     if (!m || !wavelet || !dobs || !grad) return set_err(USCT_ERR_ARG, "null argument");
     usct_plan* p = nullptr;
     TRY(host_plan(&p, dims, ndim, h, dt, nt, tx_lin, n_tx, rec_lin, n_rec));
@@ -1281,9 +1296,9 @@ extern "C" int usct_misfit_and_gradient(const double* m, const int* dims, int nd
     CUDA_TRY(cudaMemcpy(dm.p, m, p->N * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(dw.p, wavelet, (size_t)nt * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(dob.p, hdobs.data(), nd * sizeof(float), cudaMemcpyHostToDevice));
-    TRY(usct_misfit_and_gradient_dev(p, (const double*)dm.p, nullptr, (const double*)dw.p,
-                                     (const float*)dob.p, (double*)dJ.p, (double*)dg.p, mws.p,
-                                     bws.p, nullptr));
+    TRY(usct_misfit_and_gradient_mt_dev(p, (const double*)dm.p, nullptr, (const double*)dw.p,
+                                        (const float*)dob.p, misfit_type, (double*)dJ.p,
+                                        (double*)dg.p, mws.p, bws.p, nullptr));
     std::vector<double> hJ(n_tx);
     CUDA_TRY(cudaMemcpy(hJ.data(), dJ.p, (size_t)n_tx * sizeof(double), cudaMemcpyDeviceToHost));
     CUDA_TRY(cudaMemcpy(grad, dg.p, p->N * sizeof(double), cudaMemcpyDeviceToHost));

@@ -214,6 +214,14 @@ def test_host_pointer_abi_matches_reference_core():
                                             g.ctypes.data_as(_lib._dp), ctypes.byref(J)))
     assert abs(J.value - float(c["J_cpp"])) <= 1e-4 * float(c["J_cpp"])
     assert rel_l2(g, c["g_cpp"]) < 1e-4
+    _lib.check(lib.usct_misfit_and_gradient_mt(m0.ctypes.data_as(_lib._dp), dims, 3, c.h, c.dt,
+                                               c.nt, tx.ctypes.data_as(_lib._ip), len(tx),
+                                               rec.ctypes.data_as(_lib._ip), len(rec),
+                                               c.wavelet.ctypes.data_as(_lib._dp),
+                                               dobs.ctypes.data_as(_lib._dp),
+                                               g.ctypes.data_as(_lib._dp), 1, ctypes.byref(J)))
+    assert abs(J.value - float(c["J_gcn_cpp"])) <= 1e-5 * float(c["J_gcn_cpp"])
+    assert rel_l2(g, c["g_gcn_cpp"]) < 1e-4
 
 
 def test_directional_derivatives_eight_seeded_directions():
@@ -275,3 +283,27 @@ def test_error_conventions():
     with pytest.raises(ValueError):
         gb().misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"][:1],
                                  src_list=c.src_list)
+
+
+def test_backend_protocol_as_invert_calls_it():
+    """fwi.invert calls a backend positionally (fwi.py:598-603):
+    misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge, src_list,
+    misfit_type=...) and misfit(same...)."""
+    c = load("parity2d")
+    mg = gb().misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"], None,
+                                  c.src_list, misfit_type="l2")
+    mf = gb().misfit(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"], None, c.src_list,
+                     misfit_type="l2")
+    assert isinstance(mg[0], float) and mg[1].shape == c["m0"].shape
+    assert abs(mf - mg[0]) <= 1e-9 * mg[0]
+
+
+def test_simulate_dataset_on_the_gpu():
+    from openusct_gb300 import acquire
+    from openusct_gb300.geometry import RingGeometry
+    c = load("ring2d_point")
+    ring = RingGeometry(8, 0.024, 0.06, 1e-3)
+    ds = acquire.simulate_dataset(1.0 / np.sqrt(c["m_true"]), ring, c.wavelet, c.dt, 1480.0,
+                                  src_list=c.src_list)
+    assert ds.data.shape == c["dobs"].shape
+    assert rel_l2(ds.data, c["dobs"]) < 1e-5
