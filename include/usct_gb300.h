@@ -158,6 +158,17 @@ int usct_batch_misfit(usct_plan* plan, void* batch_ws, int b, const float* dobs,
 int usct_batch_misfit_mt(usct_plan* plan, void* batch_ws, int b, const float* dobs,
                          int misfit_type, double* J, void* stream);
 
+/*
+ * Misfit of batch b on windowed data (fwi.py:247-263, 298-301 time_weights):
+ * weights is a device FP32 [n_tx][nt][n_rx] window (NULL = none, then this is
+ * usct_batch_misfit_mt).  The misfit is taken between dsyn*W and dobs*W and
+ * the adjoint source is multiplied by W again (the chain rule through the
+ * window).  No counterpart in libuap, which has no windows; the Python
+ * reference's time_weights[i] is row i of weights.
+ */
+int usct_batch_misfit_tw(usct_plan* plan, void* batch_ws, int b, const float* dobs,
+                         const float* weights, int misfit_type, double* J, void* stream);
+
 /* Use an arbitrary adjoint source for batch b (device FP32 [n_tx][nt][n_rx]),
  * e.g. dL/d(traces) from an autograd graph. */
 int usct_batch_adjoint_source(usct_plan* plan, void* batch_ws, int b, const float* adj,
@@ -192,6 +203,12 @@ int usct_misfit_and_gradient_mt_dev(usct_plan* plan, const double* m, const doub
                                     const double* wavelet, const float* dobs, int misfit_type,
                                     double* J, double* grad, void* model_ws, void* batch_ws,
                                     void* stream);
+/* fwi.misfit_and_gradient with time_weights (fwi.py:266-301): weights device
+ * FP32 [n_tx][nt][n_rx] (NULL = none, then this is the _mt call). */
+int usct_misfit_and_gradient_tw_dev(usct_plan* plan, const double* m, const double* sponge,
+                                    const double* wavelet, const float* dobs,
+                                    const float* weights, int misfit_type, double* J,
+                                    double* grad, void* model_ws, void* batch_ws, void* stream);
 /* fwi.gn_hessian_vector: hv device FP64 dims-shaped; born (NULL = skip) FP32
  * [n_tx][nt][n_rx] receives J v. */
 int usct_gn_hessian_vector_dev(usct_plan* plan, const double* m, const double* sponge,
@@ -259,6 +276,41 @@ int usct_forward_fmc_noalloc(int ndim, const int* dims, double h, double dt, int
                              const int64_t* rx_cell, const double* rx_w, const double* m,
                              const double* sponge, const double* wavelet, float* data,
                              void* stream);
+
+/* ---- the model-update loop of fwi.invert on the device ---- */
+/*
+ * The whole-model FP64 operations fwi.invert (fwi.py:535-660) and its
+ * Gauss-Newton variant (fwi.py:434-532) apply between gradients, so the model
+ * and gradient stay in device memory across iterations.  All arrays are device
+ * FP64 of n (= cells) elements; NULL optional arrays mean "absent".
+ * Elementwise results round as the NumPy expressions they replace; dot and sum
+ * use a fixed order (reproducible, not NumPy's order); max|x| is exact.
+ */
+#define USCT_SMOOTH_MAX_RADIUS 64
+/* scipy.ndimage.gaussian_filter with mode 'reflect' (fwi.py:633-634): one 1-D
+ * pass per axis in axis order, each adding taps in scipy's order for a
+ * symmetric kernel.  taps (host, radius+1 values): taps[0] the centre weight,
+ * taps[j] the weight at distance j.  in, out, tmp distinct (tmp unused for
+ * ndim 1). */
+int usct_smooth_dev(const double* in, double* out, double* tmp, int ndim, const int* dims,
+                    const double* taps, int radius, void* stream);
+/* out = x * mask (mask NULL: out = x). */
+int usct_vec_mul_dev(const double* x, const double* mask, double* out, size_t n, void* stream);
+/* out = y + a * x (y NULL: out = a * x); out may alias x or y. */
+int usct_vec_axpy_dev(const double* y, double a, const double* x, double* out, size_t n,
+                      void* stream);
+/* The trial model of the line search (fwi.py:641-646, 510-513):
+ * out = m + a * d, clipped to [lo, hi] where mask > 0 (everywhere when mask is
+ * NULL; nowhere when lo and hi are NULL). */
+int usct_model_trial_dev(const double* m, double a, const double* d, const double* lo,
+                         const double* hi, const double* mask, double* out, size_t n,
+                         void* stream);
+/* *out (device) = max_i |x_i| (fwi.py:637). */
+int usct_vec_absmax_dev(const double* x, size_t n, double* out, void* stream);
+/* ws[0] (device) = sum_i x_i y_i (y NULL: sum_i x_i); ws holds
+ * USCT_DOT_WS_DOUBLES doubles. */
+#define USCT_DOT_WS_DOUBLES 609
+int usct_vec_dot_dev(const double* x, const double* y, size_t n, double* ws, void* stream);
 
 #ifdef __cplusplus
 }

@@ -25,6 +25,9 @@ MODE_FORWARD = 0
 MODE_GRADIENT = 1
 MODE_BORN = 2
 
+SMOOTH_MAX_RADIUS = 64      # USCT_SMOOTH_MAX_RADIUS
+DOT_WS_DOUBLES = 609        # USCT_DOT_WS_DOUBLES
+
 INFO = {"batch": 0, "nbatch": 1, "ckpt_k": 2, "nseg": 3, "tile_x": 4, "tile_y": 5,
         "zchunk": 6, "level_floats": 7, "launches": 8, "variant": 9}
 SET = {"variant": 0, "stages": 1, "stages_adj": 2, "graphs": 3, "wait_test": 4}
@@ -52,6 +55,7 @@ SIGNATURES = {
     "usct_batch_forward": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
     "usct_batch_misfit": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),
     "usct_batch_misfit_mt": (_i, [_vp, _vp, _i, _vp, _i, _vp, _vp]),
+    "usct_batch_misfit_tw": (_i, [_vp, _vp, _i, _vp, _vp, _i, _vp, _vp]),
     "usct_batch_adjoint_source": (_i, [_vp, _vp, _i, _vp, _vp]),
     "usct_batch_backward": (_i, [_vp, _vp, _vp, _i, _vp]),
     "usct_model_gradient": (_i, [_vp, _vp, _vp, _vp, _vp]),
@@ -59,7 +63,15 @@ SIGNATURES = {
     "usct_misfit_and_gradient_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "usct_misfit_and_gradient_mt_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp,
                                              _vp]),
+    "usct_misfit_and_gradient_tw_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp,
+                                             _vp, _vp]),
     "usct_gn_hessian_vector_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "usct_smooth_dev": (_i, [_vp, _vp, _vp, _i, _ip, _dp, _i, _vp]),
+    "usct_vec_mul_dev": (_i, [_vp, _vp, _vp, ctypes.c_size_t, _vp]),
+    "usct_vec_axpy_dev": (_i, [_vp, _d, _vp, _vp, ctypes.c_size_t, _vp]),
+    "usct_model_trial_dev": (_i, [_vp, _d, _vp, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp]),
+    "usct_vec_absmax_dev": (_i, [_vp, ctypes.c_size_t, _vp, _vp]),
+    "usct_vec_dot_dev": (_i, [_vp, _vp, ctypes.c_size_t, _vp, _vp]),
     "usct_plain_bytes": (ctypes.c_size_t, [_vp, _i]),
     "usct_plain_forward_fmc_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "usct_plain_misfit_and_gradient_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

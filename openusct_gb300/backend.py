@@ -253,15 +253,32 @@ def _out(x, like):
 _MISFIT_CODES = {"l2": 0, "gcn": 1}
 
 
-def _check_misfit(misfit_type, time_weights):
+def _check_misfit(misfit_type):
     """Returns the engine's code for misfit_type (l2 = 0, gcn = 1, as uap.py:41)."""
     if misfit_type not in _KNOWN_MISFITS:
         raise ValueError(f"unknown misfit_type {misfit_type!r}")
     if misfit_type not in _MISFIT_CODES:
         raise NotImplementedError("the GB300 backend implements the l2 and gcn misfits")
-    if time_weights is not None:
-        raise NotImplementedError("time_weights are not supported by the GB300 backend")
     return _MISFIT_CODES[misfit_type]
+
+
+def _time_weights(time_weights, plan, dev):
+    """The per-transmit data windows of fwi.py:250-259 as one device FP32
+    (n_tx, nt, n_rx) array: entry i windows the i-th transmit of src_list.
+    Accepts a list of (nt, n_rx) arrays or one stacked array/tensor."""
+    if time_weights is None:
+        return None
+    if torch.is_tensor(time_weights):
+        w = time_weights.to(device=dev, dtype=torch.float32)
+    else:
+        if isinstance(time_weights, (list, tuple)):
+            time_weights = np.stack([np.asarray(t, dtype=np.float64) for t in time_weights])
+        w = torch.from_numpy(np.ascontiguousarray(time_weights, dtype=np.float32)).to(dev)
+    want = (plan.n_tx, plan.nt, plan.n_rx)
+    if tuple(w.shape) != want:
+        raise ValueError(f"time_weights have shape {tuple(w.shape)}, expected {want} "
+                         "(one (nt, n_rx) window per transmit)")
+    return w.contiguous()
 
 
 # ---------------------------------------------------------------------------
@@ -291,8 +308,12 @@ def forward_fmc(m, geom, wavelet, dt, h, nt, sponge=None, src_list=None, footpri
 def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None,
                         misfit_type="l2", footprints=None, time_weights=None, *, batch=None,
                         ckpt_k=None, tile=None, return_per_shot=False):
-    """Waveform misfit (l2 or gcn) and its exact discrete-adjoint gradient in m (FP64)."""
-    mt = _check_misfit(misfit_type, time_weights)
+    """Waveform misfit (l2 or gcn) and its exact discrete-adjoint gradient in m (FP64).
+
+    ``time_weights`` windows the data per transmit (fwi.py:298-301): the misfit
+    compares dsyn*W with dobs*W and the adjoint source is multiplied by W.
+    """
+    mt = _check_misfit(misfit_type)
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_GRADIENT, batch, ckpt_k,
                   tile)
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -303,14 +324,15 @@ def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list
     if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
         raise ValueError(f"dobs has shape {tuple(od.shape)}, expected "
                          f"{(plan.n_tx, plan.nt, plan.n_rx)}")
+    tw = _time_weights(time_weights, plan, dev)
     J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
     g = torch.empty(plan.shape, dtype=torch.float64, device=dev)
     mws = plan.workspace("model", plan.model_bytes(), dev)
     bws = plan.workspace(_lib.MODE_GRADIENT, plan.batch_bytes(_lib.MODE_GRADIENT), dev)
     with _on_exec_stream() as st:
-        _lib.check(plan._lib.usct_misfit_and_gradient_mt_dev(
-            plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(od), mt, _ptr(J), _ptr(g), _ptr(mws),
-            _ptr(bws), _stream(st)))
+        _lib.check(plan._lib.usct_misfit_and_gradient_tw_dev(
+            plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(od), _ptr(tw), mt, _ptr(J), _ptr(g),
+            _ptr(mws), _ptr(bws), _stream(st)))
         plan.check(st)
     Jh = J.cpu().numpy()
     Jv = float(np.sum(Jh))
@@ -321,8 +343,9 @@ def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list
 
 def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, misfit_type="l2",
            footprints=None, time_weights=None, *, batch=None, tile=None):
-    """Waveform misfit (l2 or gcn) only: one forward sweep per batch."""
-    mt = _check_misfit(misfit_type, time_weights)
+    """Waveform misfit (l2 or gcn) only: one forward sweep per batch (``time_weights``
+    as in :func:`misfit_and_gradient`)."""
+    mt = _check_misfit(misfit_type)
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_FORWARD, batch, None, tile)
     dev = torch.device("cuda", torch.cuda.current_device())
     md = _to_dev(m, torch.float64, dev)
@@ -331,6 +354,7 @@ def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, misfit
     od = _to_dev(dobs, torch.float32, dev)
     if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
         raise ValueError("dobs shape does not match the acquisition")
+    tw = _time_weights(time_weights, plan, dev)
     J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
     mws = plan.workspace("model", plan.model_bytes(), dev)
     bws = plan.workspace(_lib.MODE_FORWARD, plan.batch_bytes(_lib.MODE_FORWARD), dev)
@@ -342,8 +366,8 @@ def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, misfit
         for b in range(plan.nbatch):
             _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
                                               _lib.MODE_FORWARD, None, s))
-            _lib.check(lib.usct_batch_misfit_mt(plan.handle, _ptr(bws), b, _ptr(od), mt, _ptr(J),
-                                                s))
+            _lib.check(lib.usct_batch_misfit_tw(plan.handle, _ptr(bws), b, _ptr(od), _ptr(tw),
+                                                mt, _ptr(J), s))
         plan.check(st)
     return float(np.sum(J.cpu().numpy()))
 

@@ -1,6 +1,6 @@
 """Build recipe for the CUDA library ``openusct_gb300/libusct_gb300.so``.
 
-Two translation units, one ``-gencode`` (sm_103a), built in-tree with nvcc.
+Three translation units, one ``-gencode`` (sm_103a), built in-tree with nvcc.
 ``-fmad=false`` keeps every multiply-add unfused unless the kernels ask for
 ``__fmaf_rn`` explicitly, which fixes the rounding of the stencil so the CPU
 restatement can reproduce it bit for bit.
@@ -16,8 +16,9 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "libusct_gb300.so")
-SOURCES = ["usct_engine.cu", "usct_noalloc.cu"]
-DEPS = ["usct_engine.cu", "usct_noalloc.cu", "usct_kernels.cuh", "usct_plain.cuh", "usct_tma.cuh"]
+SOURCES = ["usct_engine.cu", "usct_noalloc.cu", "usct_invert.cu"]
+DEPS = ["usct_engine.cu", "usct_noalloc.cu", "usct_invert.cu", "usct_kernels.cuh", "usct_plain.cuh",
+        "usct_tma.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -28,13 +29,20 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libusct_gb300.so")
 
 
-def command(out: str = LIB, verbose_ptxas: bool = False) -> list[str]:
+OBJDIR = os.path.join(PKG, "_build")
+
+
+def compile_command(src: str, obj: str, verbose_ptxas: bool = False) -> list[str]:
     cmd = [nvcc(), ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17",
-           "-Xcompiler", "-fPIC", "-shared", "-I", os.path.join(REPO, "include"),
-           "-o", out] + [os.path.join(CSRC, s) for s in SOURCES]
+           "-Xcompiler", "-fPIC", "-I", os.path.join(REPO, "include"),
+           "-c", "-o", obj, os.path.join(CSRC, src)]
     if verbose_ptxas:
         cmd.insert(1, "-Xptxas=-v")
     return cmd
+
+
+def link_command(objs: list[str], out: str) -> list[str]:
+    return [nvcc(), ARCH, "-shared", "-o", out] + objs
 
 
 def up_to_date(out: str = LIB) -> bool:
@@ -46,10 +54,20 @@ def up_to_date(out: str = LIB) -> bool:
 
 
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
-    """Compile the library if a source is newer than it; return its path."""
+    """Compile the library if a source is newer than it; return its path.
+
+    The translation units compile in parallel (one nvcc each), then link."""
     if force or not up_to_date():
+        os.makedirs(OBJDIR, exist_ok=True)
+        objs = [os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o") for src in SOURCES]
+        procs = [subprocess.Popen(compile_command(src, obj, verbose_ptxas))
+                 for src, obj in zip(SOURCES, objs)]
+        codes = [p.wait() for p in procs]
+        if any(codes):
+            raise subprocess.CalledProcessError(next(c for c in codes if c),
+                                                compile_command(SOURCES[0], objs[0]))
         tmp = LIB + ".tmp"
-        subprocess.run(command(tmp, verbose_ptxas), check=True)
+        subprocess.run(link_command(objs, tmp), check=True)
         os.replace(tmp, LIB)
     return LIB
 

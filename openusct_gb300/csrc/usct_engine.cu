@@ -485,7 +485,8 @@ __global__ void __launch_bounds__(256) k_gather(const float* __restrict__ rs, in
                                                 int nt, int nrx, const int* __restrict__ rx_ptr,
                                                 int shot0, int nb, float* out,
                                                 const float* __restrict__ dobs, float* res,
-                                                int mode, double* jpart) {
+                                                int mode, double* jpart,
+                                                const float* __restrict__ tw) {
     __shared__ double sj[256];
     const int tid = threadIdx.x;
     const int c = tid & (C - 1);
@@ -503,11 +504,19 @@ __global__ void __launch_bounds__(256) k_gather(const float* __restrict__ rs, in
             const long long uo = ((long long)(shot0 + c) * nt + n) * nrx + j;
             if (out) out[uo] = tr;
             if (mode == 1) {
-                const float rr = tr - dobs[uo];
-                res[r * C + c] = rr;
-                J += 0.5 * (double)rr * (double)rr;
+                if (tw) {
+                    // windowed data (fwi.py:298-301): r = dsyn W - dobs W, adjoint source r W
+                    const float wv = tw[uo];
+                    const float rr = tr * wv - dobs[uo] * wv;
+                    res[r * C + c] = rr * wv;
+                    J += 0.5 * (double)rr * (double)rr;
+                } else {
+                    const float rr = tr - dobs[uo];
+                    res[r * C + c] = rr;
+                    J += 0.5 * (double)rr * (double)rr;
+                }
             } else if (mode == 2) {
-                res[r * C + c] = tr;
+                res[r * C + c] = tw ? tr * tw[uo] : tr;
             }
         } else if (mode) {
             res[r * C + c] = 0.f;
@@ -545,9 +554,11 @@ __global__ void k_adjsrc(const float* __restrict__ adj, float* res, int C, int n
 
 // GCN adjoint source (libuap.hpp:133-162, fwi.py:158-167) from the traces in
 // res ([nt][n_rx][C]), in place: per (receiver j, shot c) FP64 sums over time
-// of the FP32 traces; gj[j][c] = 1 - c_j for the per-shot misfit.
+// of the FP32 traces; gj[j][c] = 1 - c_j for the per-shot misfit.  With a
+// window tw the traces in res are already windowed, dobs is windowed here and
+// the adjoint source is multiplied by the window (fwi.py:298-301).
 __global__ void k_gcn(float* res, const float* __restrict__ dobs, int C, int logC, int nt, int nrx,
-                      int shot0, int nb, double* gj) {
+                      int shot0, int nb, double* gj, const float* __restrict__ tw) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= nrx * C) return;
     const int j = idx >> logC, c = idx & (C - 1);
@@ -559,11 +570,16 @@ __global__ void k_gcn(float* res, const float* __restrict__ dobs, int C, int log
         return;
     }
     const float* ob = dobs + (long long)(shot0 + c) * nt * nrx + j;
+    const float* wb = tw ? tw + (long long)(shot0 + c) * nt * nrx + j : nullptr;
+    auto obs = [&](int n) -> double {
+        const long long o = (long long)n * nrx;
+        return wb ? (double)(ob[o] * wb[o]) : (double)ob[o];
+    };
     const double eps = 1e-12;
     double sn = 0.0, on = 0.0;
     for (int n = 0; n < nt; ++n) {
         const double sv = (double)col[n * rstride];
-        const double ov = (double)ob[(long long)n * nrx];
+        const double ov = obs(n);
         sn += sv * sv;
         on += ov * ov;
     }
@@ -572,13 +588,14 @@ __global__ void k_gcn(float* res, const float* __restrict__ dobs, int C, int log
     double cc = 0.0;
     for (int n = 0; n < nt; ++n) {
         const double sv = (double)col[n * rstride];
-        const double ov = (double)ob[(long long)n * nrx];
+        const double ov = obs(n);
         cc += (sv / sn) * (ov / on);
     }
     for (int n = 0; n < nt; ++n) {
         const double sv = (double)col[n * rstride];
-        const double ov = (double)ob[(long long)n * nrx];
-        col[n * rstride] = (float)(-(ov / on - cc * (sv / sn)) / sn);
+        const double ov = obs(n);
+        const float adj = (float)(-(ov / on - cc * (sv / sn)) / sn);
+        col[n * rstride] = wb ? adj * wb[(long long)n * nrx] : adj;
     }
     gj[idx] = 1.0 - cc;
 }
@@ -934,11 +951,11 @@ extern "C" int usct_model_gradient(usct_plan* p, void* model_ws, const double* m
 // batch sweeps
 // ---------------------------------------------------------------------------
 static int gather(usct_plan* p, const BatchWS& B, int b, float* out, const float* dobs, int mode,
-                  cudaStream_t s) {
+                  cudaStream_t s, const float* tw = nullptr) {
     const int shot0 = b * p->C;
     const int nb = std::min(p->C, p->n_tx - shot0);
     k_gather<<<JBLK, 256, 0, s>>>(B.rs, p->nslot, p->C, p->logC, p->nt, p->n_rx, p->d_rxptr, shot0,
-                                  nb, out, dobs, B.res, mode, B.jpart);
+                                  nb, out, dobs, B.res, mode, B.jpart, tw);
     ++p->launches;
     CUDA_TRY(cudaGetLastError());
     return USCT_OK;
@@ -1045,11 +1062,18 @@ static int batch_forward_impl(usct_plan* p, const void* model_ws, void* batch_ws
 
 extern "C" int usct_batch_misfit(usct_plan* p, void* batch_ws, int b, const float* dobs, double* J,
                                  void* stream) {
-    if (!p || !batch_ws || !dobs) return set_err(USCT_ERR_ARG, "null argument");
-    if (b < 0 || b >= p->nbatch) return set_err(USCT_ERR_ARG, "batch %d out of range", b);
-    cudaStream_t s = (cudaStream_t)stream;
+    return usct_batch_misfit_tw(p, batch_ws, b, dobs, nullptr, 0, J, stream);
+}
+
+extern "C" int usct_batch_misfit_mt(usct_plan* p, void* batch_ws, int b, const float* dobs,
+                                    int misfit_type, double* J, void* stream) {
+    return usct_batch_misfit_tw(p, batch_ws, b, dobs, nullptr, misfit_type, J, stream);
+}
+
+static int batch_misfit_l2(usct_plan* p, void* batch_ws, int b, const float* dobs,
+                           const float* tw, double* J, cudaStream_t s) {
     const BatchWS B = carve_batch(p, batch_ws, USCT_MODE_FORWARD);
-    TRY(gather(p, B, b, nullptr, dobs, 1, s));
+    TRY(gather(p, B, b, nullptr, dobs, 1, s, tw));
     if (J) {
         const int shot0 = b * p->C;
         const int nb = std::min(p->C, p->n_tx - shot0);
@@ -1060,19 +1084,22 @@ extern "C" int usct_batch_misfit(usct_plan* p, void* batch_ws, int b, const floa
     return USCT_OK;
 }
 
-extern "C" int usct_batch_misfit_mt(usct_plan* p, void* batch_ws, int b, const float* dobs,
-                                    int misfit_type, double* J, void* stream) {
-    if (misfit_type == 0) return usct_batch_misfit(p, batch_ws, b, dobs, J, stream);
-    if (misfit_type != 1) return set_err(USCT_ERR_ARG, "misfit_type must be 0 (L2) or 1 (GCN)");
+extern "C" int usct_batch_misfit_tw(usct_plan* p, void* batch_ws, int b, const float* dobs,
+                                    const float* weights, int misfit_type, double* J,
+                                    void* stream) {
     if (!p || !batch_ws || !dobs) return set_err(USCT_ERR_ARG, "null argument");
+    if (misfit_type != 0 && misfit_type != 1)
+        return set_err(USCT_ERR_ARG, "misfit_type must be 0 (L2) or 1 (GCN)");
     if (b < 0 || b >= p->nbatch) return set_err(USCT_ERR_ARG, "batch %d out of range", b);
     cudaStream_t s = (cudaStream_t)stream;
+    if (misfit_type == 0) return batch_misfit_l2(p, batch_ws, b, dobs, weights, J, s);
     const BatchWS B = carve_batch(p, batch_ws, USCT_MODE_FORWARD);
-    TRY(gather(p, B, b, nullptr, nullptr, 2, s));   // res = traces
+    TRY(gather(p, B, b, nullptr, nullptr, 2, s, weights));   // res = (windowed) traces
     const int shot0 = b * p->C;
     const int nb = std::min(p->C, p->n_tx - shot0);
     const int n = p->n_rx * p->C;
-    k_gcn<<<(n + 127) / 128, 128, 0, s>>>(B.res, dobs, p->C, p->logC, p->nt, p->n_rx, shot0, nb, B.gj);
+    k_gcn<<<(n + 127) / 128, 128, 0, s>>>(B.res, dobs, p->C, p->logC, p->nt, p->n_rx, shot0, nb, B.gj,
+                                          weights);
     ++p->launches;
     if (J) {
         k_gcn_j<<<1, 64, 0, s>>>(B.gj, p->C, p->n_rx, shot0, nb, J);
@@ -1187,12 +1214,21 @@ extern "C" int usct_misfit_and_gradient_mt_dev(usct_plan* p, const double* m, co
                                                const double* wavelet, const float* dobs,
                                                int misfit_type, double* J, double* grad,
                                                void* model_ws, void* batch_ws, void* stream) {
+    return usct_misfit_and_gradient_tw_dev(p, m, sponge, wavelet, dobs, nullptr, misfit_type, J,
+                                           grad, model_ws, batch_ws, stream);
+}
+
+extern "C" int usct_misfit_and_gradient_tw_dev(usct_plan* p, const double* m, const double* sponge,
+                                               const double* wavelet, const float* dobs,
+                                               const float* weights, int misfit_type, double* J,
+                                               double* grad, void* model_ws, void* batch_ws,
+                                               void* stream) {
     if (misfit_type != 0 && misfit_type != 1)
         return set_err(USCT_ERR_ARG, "misfit_type must be 0 (L2) or 1 (GCN)");
     TRY(usct_model_prepare(p, model_ws, m, sponge, nullptr, wavelet, stream));
     for (int b = 0; b < p->nbatch; ++b) {
         TRY(usct_batch_forward(p, model_ws, batch_ws, b, USCT_MODE_GRADIENT, nullptr, stream));
-        TRY(usct_batch_misfit_mt(p, batch_ws, b, dobs, misfit_type, J, stream));
+        TRY(usct_batch_misfit_tw(p, batch_ws, b, dobs, weights, misfit_type, J, stream));
         TRY(usct_batch_backward(p, model_ws, batch_ws, b, stream));
     }
     return usct_model_gradient(p, model_ws, m, grad, stream);

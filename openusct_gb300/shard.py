@@ -22,10 +22,12 @@ def shard(n_items, rank, world):
 
 
 def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None,
-                        misfit_type="l2", footprints=None, *, group=None, compute=None, **kw):
+                        misfit_type="l2", footprints=None, time_weights=None, *, group=None,
+                        compute=None, **kw):
     """Sharded L2/GCN misfit and gradient; every rank returns the full (J, g).
 
     ``compute`` defaults to :func:`openusct_gb300.backend.misfit_and_gradient`.
+    ``time_weights`` (one window per transmit) is split with the transmits.
     """
     import torch
     import torch.distributed as dist
@@ -37,6 +39,8 @@ def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list
     mine = shard(len(shots), rank, world)
     shape = tuple(np.shape(m))
     if mine:
+        if time_weights is not None:
+            kw["time_weights"] = [time_weights[i] for i in mine]
         J, g = compute(m, geom, wavelet, dt, h, nt, np.asarray(dobs)[mine], sponge,
                        [shots[i] for i in mine], misfit_type=misfit_type, footprints=footprints,
                        **kw)

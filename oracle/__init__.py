@@ -54,6 +54,7 @@ def _load():
             lib = ctypes.CDLL(_LIB)
             lib.usct_oracle_misfit_and_gradient.restype = ctypes.c_double
             lib.usct_oracle_misfit_and_gradient_mt.restype = ctypes.c_double
+            lib.usct_oracle_misfit_and_gradient_tw.restype = ctypes.c_double
             _lib = lib
     return _lib
 
@@ -137,35 +138,55 @@ def forward_fmc(m, geom, wavelet, dt, h, nt, sponge=None, src_list=None, footpri
 _MT = {"l2": 0, "gcn": 1}
 
 
+def _windows(time_weights, shape):
+    """time_weights (fwi.py:250-253: one (nt, n_rx) window per transmit) as a
+    contiguous float64 (n_tx, nt, n_rx) array, or None."""
+    if time_weights is None:
+        return None
+    w = np.ascontiguousarray(np.stack([np.asarray(t, np.float64) for t in time_weights]))
+    if w.shape != tuple(shape):
+        raise ValueError(f"time_weights shape {w.shape} != {tuple(shape)}")
+    return w
+
+
 def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None,
-                        footprints=None, k=0, misfit_type="l2"):
-    """FP64 restatement of fwi.misfit_and_gradient (L2 or GCN).  k = 0: full
-    history (the reference's memory plan); k > 0: checkpoints every k steps."""
+                        footprints=None, k=0, misfit_type="l2", time_weights=None):
+    """FP64 restatement of fwi.misfit_and_gradient (L2 or GCN, optional
+    time_weights as fwi.py:298-301).  k = 0: full history (the reference's
+    memory plan); k > 0: checkpoints every k steps."""
     lib = _load()
     m, dims, wav, sp = _common(m, wavelet, sponge)
     (tp, ti, tw), (rp, ri, rw), ntx, nrx = _geometry(geom, m.shape, src_list, footprints)
     dobs = np.ascontiguousarray(dobs, np.float64)
+    win = _windows(time_weights, (ntx, nt, nrx))
     g = np.zeros(m.shape)
-    J = lib.usct_oracle_misfit_and_gradient_mt(
+    J = lib.usct_oracle_misfit_and_gradient_tw(
         _p(m, _dp), _p(dims, _ip), m.ndim, ctypes.c_double(h), ctypes.c_double(dt), int(nt),
         ntx, _p(tp, _ip), _p(ti, _lp), _p(tw, _dp), nrx, _p(rp, _ip), _p(ri, _lp), _p(rw, _dp),
-        _p(wav, _dp), None if sp is None else _p(sp, _dp), _p(dobs, _dp), _p(g, _dp), int(k),
-        _MT[misfit_type])
+        _p(wav, _dp), None if sp is None else _p(sp, _dp), _p(dobs, _dp),
+        None if win is None else _p(win, _dp), _p(g, _dp), int(k), _MT[misfit_type])
     return float(J), g
 
 
 def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, footprints=None,
-           misfit_type="l2"):
+           misfit_type="l2", time_weights=None):
+    """FP64 fwi.misfit (fwi.py:246-263): forward FMC, then the per-transmit
+    misfit of the (optionally windowed) traces."""
     d = forward_fmc(m, geom, wavelet, dt, h, nt, sponge, src_list, footprints)
+    dobs = np.asarray(dobs, np.float64)
+    win = _windows(time_weights, d.shape)
     J = 0.0
     for i in range(d.shape[0]):
+        di, oi = d[i], dobs[i]
+        if win is not None:
+            di, oi = di * win[i], oi * win[i]
         if misfit_type == "gcn":   # libuap.hpp:133-154
             eps = 1e-12
-            ns = np.sqrt(np.sum(d[i] * d[i], axis=0)) + eps
-            no = np.sqrt(np.sum(dobs[i] * dobs[i], axis=0)) + eps
-            J += float(np.sum(1.0 - np.sum((d[i] / ns) * (dobs[i] / no), axis=0)))
+            ns = np.sqrt(np.sum(di * di, axis=0)) + eps
+            no = np.sqrt(np.sum(oi * oi, axis=0)) + eps
+            J += float(np.sum(1.0 - np.sum((di / ns) * (oi / no), axis=0)))
         else:
-            r = d[i] - dobs[i]
+            r = di - oi
             J += 0.5 * float(np.sum(r * r))
     return J
 
@@ -218,20 +239,22 @@ def forward_fmc32(m, geom, wavelet, dt, h, nt, sponge=None, src_list=None, footp
 
 
 def misfit_and_gradient32(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None,
-                          footprints=None, C=1, misfit_type="l2"):
+                          footprints=None, C=1, misfit_type="l2", time_weights=None):
     """Returns (J per transmit float64 array, g float64) in kernel order for a
     batch width of C shot channels."""
     lib = _load()
     m, dims, wav, sp = _common(m, wavelet, sponge)
     (tp, ti, tw), (rp, ri, rw), ntx, nrx = _geometry(geom, m.shape, src_list, footprints)
     dobs = np.ascontiguousarray(dobs, np.float64)
+    win = _windows(time_weights, (ntx, nt, nrx))
     g = np.zeros(m.shape)
     J = np.zeros(ntx)
-    rc = lib.usct_oracle32_misfit_and_gradient_mt(
+    rc = lib.usct_oracle32_misfit_and_gradient_tw(
         _p(m, _dp), _p(dims, _ip), m.ndim, ctypes.c_double(h), ctypes.c_double(dt), int(nt),
         ntx, _p(tp, _ip), _p(ti, _lp), _p(tw, _dp), nrx, _p(rp, _ip), _p(ri, _lp), _p(rw, _dp),
-        _p(wav, _dp), None if sp is None else _p(sp, _dp), _p(dobs, _dp), int(C), _p(J, _dp),
-        _p(g, _dp), _MT[misfit_type])
+        _p(wav, _dp), None if sp is None else _p(sp, _dp), _p(dobs, _dp),
+        None if win is None else _p(win, _dp), int(C), _p(J, _dp), _p(g, _dp),
+        _MT[misfit_type])
     if rc != 0:
         raise ValueError("C must be a power of two <= 64")
     return J, g

@@ -314,6 +314,13 @@ double usct_oracle_misfit_and_gradient(const double* m, const int* dims, int ndi
                                               kck, 0);
 }
 
+double usct_oracle_misfit_and_gradient_tw(const double* m, const int* dims, int ndim, double h,
+                                          double dt, int nt, int n_tx, const int* tx_ptr,
+                                          const i64* tx_idx, const double* tx_w, int nrx,
+                                          const int* rx_ptr, const i64* rx_idx, const double* rx_w,
+                                          const double* wav, const double* sponge, const double* dobs,
+                                          const double* tw, double* grad, int kck, int misfit_type);
+
 /* misfit_type 0 = L2, 1 = GCN (libuap.hpp:169, misfit_type). */
 double usct_oracle_misfit_and_gradient_mt(const double* m, const int* dims, int ndim, double h,
                                           double dt, int nt, int n_tx, const int* tx_ptr,
@@ -321,6 +328,19 @@ double usct_oracle_misfit_and_gradient_mt(const double* m, const int* dims, int 
                                           const int* rx_ptr, const i64* rx_idx, const double* rx_w,
                                           const double* wav, const double* sponge, const double* dobs,
                                           double* grad, int kck, int misfit_type) {
+    return usct_oracle_misfit_and_gradient_tw(m, dims, ndim, h, dt, nt, n_tx, tx_ptr, tx_idx, tx_w,
+                                              nrx, rx_ptr, rx_idx, rx_w, wav, sponge, dobs, NULL,
+                                              grad, kck, misfit_type);
+}
+
+/* With per-transmit data windows tw[t][n][j] (NULL = none), fwi.py:298-301:
+ * the misfit of (dsyn W, dobs W), adjoint source multiplied by W. */
+double usct_oracle_misfit_and_gradient_tw(const double* m, const int* dims, int ndim, double h,
+                                          double dt, int nt, int n_tx, const int* tx_ptr,
+                                          const i64* tx_idx, const double* tx_w, int nrx,
+                                          const int* rx_ptr, const i64* rx_idx, const double* rx_w,
+                                          const double* wav, const double* sponge, const double* dobs,
+                                          const double* tw, double* grad, int kck, int misfit_type) {
     G64 g; double* S;
     setup64(&g, m, dims, ndim, h, dt, nt, wav, sponge, nrx, rx_ptr, rx_idx, rx_w, &S);
     const size_t N = g.N;
@@ -329,18 +349,31 @@ double usct_oracle_misfit_and_gradient_mt(const double* m, const int* dims, int 
     double* res = (double*)malloc((size_t)nt * nrx * sizeof(double));
     double* hist = kck ? NULL : (double*)malloc((size_t)nt * N * sizeof(double));
     double* ck = kck ? (double*)malloc((size_t)nseg_of(nt, kck) * 2 * N * sizeof(double)) : NULL;
+    const size_t nd = (size_t)nt * nrx;
+    double* wob = tw ? (double*)malloc(nd * sizeof(double)) : NULL;
     double J = 0.0;
     for (int t = 0; t < n_tx; ++t) {
         const int ns = tx_ptr[t + 1] - tx_ptr[t];
         forward64(&g, ns, tx_idx + tx_ptr[t], tx_w + tx_ptr[t], dsyn, hist, kck, ck);
+        const double* ob = dobs + (size_t)t * nd;
+        const double* W = tw ? tw + (size_t)t * nd : NULL;
+        if (W) {
+            for (size_t q = 0; q < nd; ++q) {
+                dsyn[q] *= W[q];
+                wob[q] = ob[q] * W[q];
+            }
+            ob = wob;
+        }
         if (misfit_type == 1)
-            J += residual64_gcn(dsyn, dobs + (size_t)t * nt * nrx, nt, nrx, res);
+            J += residual64_gcn(dsyn, ob, nt, nrx, res);
         else
-            J += residual64(dsyn, dobs + (size_t)t * nt * nrx, (size_t)nt * nrx, res);
+            J += residual64(dsyn, ob, nd, res);
+        if (W)
+            for (size_t q = 0; q < nd; ++q) res[q] *= W[q];
         backward64(&g, ns, tx_idx + tx_ptr[t], tx_w + tx_ptr[t], res, hist, kck, ck, grad);
     }
     for (size_t i = 0; i < N; ++i) grad[i] /= m[i];
-    free(S); free(dsyn); free(res); free(hist); free(ck);
+    free(S); free(dsyn); free(res); free(hist); free(ck); free(wob);
     return J;
 }
 
@@ -608,7 +641,7 @@ static int grad32_impl(const double* m, const int* dims, int ndim, double h, dou
                        int nrx, const int* rx_ptr, const i64* rx_idx, const double* rx_w,
                        const double* wav, const double* sponge, const double* dobs, int C,
                        double* J_out, double* grad, const double* born_v, float* born_out,
-                       int misfit_type) {
+                       int misfit_type, const double* tw) {
     G32 g;
     setup32(&g, m, dims, ndim, h, dt, nt, wav, sponge, nrx, rx_ptr, rx_idx, rx_w);
     const size_t N = g.N;
@@ -691,17 +724,22 @@ static int grad32_impl(const double* m, const int* dims, int ndim, double h, dou
                 }
             }
             /* adjoint source */
+            /* windows as the device applies them: FP32 products with the FP32 window */
+            const double* W = tw ? tw + (size_t)t * nt * nrx : NULL;
             if (!born_v && misfit_type == 1) {
                 /* GCN as the device computes it: per receiver, FP64 sums over time of
                  * the FP32 traces (sequential in n), J = sum_j (1 - c_j) in j order */
                 const double* ob = dobs + (size_t)t * nt * nrx;
+                if (W)
+                    for (size_t z = 0; z < (size_t)nt * nrx; ++z) dsyn[z] = dsyn[z] * (float)W[z];
+#define OBS(z) (W ? (double)((float)ob[(z)] * (float)W[(z)]) : (double)(float)ob[(z)])
                 const double eps = 1e-12;
                 double J = 0.0;
                 for (int j = 0; j < nrx; ++j) {
                     double sn = 0.0, on = 0.0, cc = 0.0;
                     for (int n = 0; n < nt; ++n) {
                         const double sv = (double)dsyn[(size_t)n * nrx + j];
-                        const double ov = (double)(float)ob[(size_t)n * nrx + j];
+                        const double ov = OBS((size_t)n * nrx + j);
                         sn += sv * sv;
                         on += ov * ov;
                     }
@@ -709,24 +747,34 @@ static int grad32_impl(const double* m, const int* dims, int ndim, double h, dou
                     on = sqrt(on) + eps;
                     for (int n = 0; n < nt; ++n) {
                         const double sv = (double)dsyn[(size_t)n * nrx + j];
-                        const double ov = (double)(float)ob[(size_t)n * nrx + j];
+                        const double ov = OBS((size_t)n * nrx + j);
                         cc += (sv / sn) * (ov / on);
                     }
                     for (int n = 0; n < nt; ++n) {
-                        const double sv = (double)dsyn[(size_t)n * nrx + j];
-                        const double ov = (double)(float)ob[(size_t)n * nrx + j];
-                        res[c][(size_t)n * nrx + j] = (float)(-(ov / on - cc * (sv / sn)) / sn);
+                        const size_t z = (size_t)n * nrx + j;
+                        const double sv = (double)dsyn[z];
+                        const double ov = OBS(z);
+                        const float adj = (float)(-(ov / on - cc * (sv / sn)) / sn);
+                        res[c][z] = W ? adj * (float)W[z] : adj;
                     }
                     J += 1.0 - cc;
                 }
+#undef OBS
                 if (J_out) J_out[t] = J;
             } else if (!born_v) {
                 const double* ob = dobs + (size_t)t * nt * nrx;
                 double J = 0.0;
                 for (size_t z = 0; z < (size_t)nt * nrx; ++z) {
-                    const float r = dsyn[z] - (float)ob[z];
-                    res[c][z] = r;
-                    J += 0.5 * (double)r * (double)r;
+                    if (W) {
+                        const float wv = (float)W[z];
+                        const float r = dsyn[z] * wv - (float)ob[z] * wv;
+                        res[c][z] = r * wv;
+                        J += 0.5 * (double)r * (double)r;
+                    } else {
+                        const float r = dsyn[z] - (float)ob[z];
+                        res[c][z] = r;
+                        J += 0.5 * (double)r * (double)r;
+                    }
                 }
                 if (J_out) J_out[t] = J;
             } else {
@@ -788,7 +836,7 @@ int usct_oracle32_misfit_and_gradient(const double* m, const int* dims, int ndim
                                       double* J_out, double* grad) {
     if (C < 1 || C > 64 || (C & (C - 1))) return -1;
     return grad32_impl(m, dims, ndim, h, dt, nt, n_tx, tx_ptr, tx_idx, tx_w, nrx, rx_ptr, rx_idx,
-                       rx_w, wav, sponge, dobs, C, J_out, grad, NULL, NULL, 0);
+                       rx_w, wav, sponge, dobs, C, J_out, grad, NULL, NULL, 0, NULL);
 }
 
 int usct_oracle32_misfit_and_gradient_mt(const double* m, const int* dims, int ndim, double h,
@@ -799,7 +847,19 @@ int usct_oracle32_misfit_and_gradient_mt(const double* m, const int* dims, int n
                                          int C, double* J_out, double* grad, int misfit_type) {
     if (C < 1 || C > 64 || (C & (C - 1))) return -1;
     return grad32_impl(m, dims, ndim, h, dt, nt, n_tx, tx_ptr, tx_idx, tx_w, nrx, rx_ptr, rx_idx,
-                       rx_w, wav, sponge, dobs, C, J_out, grad, NULL, NULL, misfit_type);
+                       rx_w, wav, sponge, dobs, C, J_out, grad, NULL, NULL, misfit_type, NULL);
+}
+
+int usct_oracle32_misfit_and_gradient_tw(const double* m, const int* dims, int ndim, double h,
+                                         double dt, int nt, int n_tx, const int* tx_ptr,
+                                         const i64* tx_idx, const double* tx_w, int nrx,
+                                         const int* rx_ptr, const i64* rx_idx, const double* rx_w,
+                                         const double* wav, const double* sponge, const double* dobs,
+                                         const double* tw, int C, double* J_out, double* grad,
+                                         int misfit_type) {
+    if (C < 1 || C > 64 || (C & (C - 1))) return -1;
+    return grad32_impl(m, dims, ndim, h, dt, nt, n_tx, tx_ptr, tx_idx, tx_w, nrx, rx_ptr, rx_idx,
+                       rx_w, wav, sponge, dobs, C, J_out, grad, NULL, NULL, misfit_type, tw);
 }
 
 int usct_oracle32_gn_hessian_vector(const double* m, const int* dims, int ndim, double h, double dt, int nt,
@@ -809,5 +869,5 @@ int usct_oracle32_gn_hessian_vector(const double* m, const int* dims, int ndim, 
                                     double* out, float* born_out) {
     if (C < 1 || C > 64 || (C & (C - 1))) return -1;
     return grad32_impl(m, dims, ndim, h, dt, nt, n_tx, tx_ptr, tx_idx, tx_w, nrx, rx_ptr, rx_idx,
-                       rx_w, wav, sponge, NULL, C, NULL, out, v, born_out, 0);
+                       rx_w, wav, sponge, NULL, C, NULL, out, v, born_out, 0, NULL);
 }

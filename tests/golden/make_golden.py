@@ -23,6 +23,16 @@ own tests:
                      C++-vs-Python parity problems)
 * gpu3d           -- software/python/test_gpu.py:139-152 (the reference's
                      FP32-GPU-vs-FP64 parity problem, every third element)
+* ring2d_window / cyl3d_window -- the ring2d_point / cyl3d_point problems with
+                     per-transmit data windows (fwi.py:247-301 time_weights): a
+                     tapered mute after the direct arrival, L2 and GCN
+* invert2d        -- fwi.invert (fwi.py:535-660) on the ring2d_point problem
+                     with an update mask and bounds as fwi_from_dataset builds
+                     them (fwi.py:753-760): 3 steepest-descent iterations (L2),
+                     2 with GCN, 2 with the ring2d_window windows, and one
+                     truncated Gauss-Newton iteration (fwi.py:434-532)
+
+``--only a,b`` regenerates just the named fixtures.
 
 Each fixture stores the inputs (m, m0, element indices, footprints as CSR,
 wavelet, dt, h, nt, src_list, sponge) and the reference outputs (dobs, J, g;
@@ -56,7 +66,12 @@ def _fp_csr(footprints):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default="")
     args = ap.parse_args()
+    only = set(filter(None, args.only.split(",")))
+
+    def want(name):
+        return not only or name in only
     sys.path.insert(0, os.path.join(args.ref, "simulation"))
     sys.path.insert(0, REPO)
     from ringfwi import fwi, phantom
@@ -75,6 +90,8 @@ def main():
 
     def point_case(name, geom, m_true, m0, wav, dt, h, nt, src_list, sponge=None,
                    with_cpp=True):
+        if not want(name):
+            return
         idx = np.asarray(geom.idx, np.int32)
         dobs = fwi.forward_fmc(m_true, geom, wav, dt, h, nt, sponge, src_list)
         J, g = fwi.misfit_and_gradient(m0, geom, wav, dt, h, nt, dobs, sponge, src_list)
@@ -99,6 +116,34 @@ def main():
             assert abs(Jc - J) <= 1e-12 * abs(J)
         save(name, **out)
 
+    def window_case(name, geom, m_true, m0, wav, dt, h, nt, src_list, c_mute, f0, periods):
+        """time_weights: W[i][n, j] = 1 up to `periods` periods after the straight-ray
+        arrival from transmit i to receiver j at c_mute, then a cosine taper to
+        0 over 40 samples (a P-arrival mute as fwi.py:250-253 describes)."""
+        if not want(name):
+            return
+        idx = np.asarray(geom.idx, np.float64)
+        t = np.arange(nt) * dt
+        W = []
+        for s in src_list:
+            dist = np.linalg.norm(idx - idx[s], axis=1) * h
+            t0 = dist / c_mute + periods / f0
+            x = np.clip((t[:, None] - t0[None, :]) / (40 * dt), 0.0, 1.0)
+            W.append(0.5 * (1.0 + np.cos(np.pi * x)))
+        W = np.asarray(W)
+        dobs = fwi.forward_fmc(m_true, geom, wav, dt, h, nt, None, src_list)
+        out = dict(m_true=m_true, m0=m0, idx=np.asarray(geom.idx, np.int32), wavelet=wav, dt=dt,
+                   h=h, nt=nt, src_list=np.asarray(src_list, np.int32), dobs=dobs,
+                   sponge=np.zeros(0), tw=W)
+        for mt, sfx in (("l2", ""), ("gcn", "_gcn")):
+            J, g = fwi.misfit_and_gradient(m0, geom, wav, dt, h, nt, dobs, None, src_list,
+                                           misfit_type=mt, time_weights=list(W))
+            out["J" + sfx] = J
+            out["g" + sfx] = g
+            out["Jm" + sfx] = fwi.misfit(m0, geom, wav, dt, h, nt, dobs, None, src_list,
+                                         misfit_type=mt, time_weights=list(W))
+        save(name, **out)
+
     # --- 2D ring, point elements (test_gradient.py) ---------------------------
     h = 1.0e-3
     geom = RingArray(n_elements=8, radius_m=0.024, domain_m=0.06, h=h)
@@ -109,6 +154,31 @@ def main():
     ct = phantom.add_inclusion(c0, (0.5, 0.5), 0.006, 3400.0, h)
     m_true, m0 = phantom.velocity_to_m(ct), phantom.velocity_to_m(c0)
     point_case("ring2d_point", geom, m_true, m0, wav, dt, h, nt, [0, 4])
+    window_case("ring2d_window", geom, m_true, m0, wav, dt, h, nt, [0, 4], 1480.0, 0.4e6, 6.0)
+
+    # --- the inversion loops (fwi.py:434-660) ----------------------------------
+    if want("invert2d"):
+        sl = [0, 4]
+        dobs = fwi.forward_fmc(m_true, geom, wav, dt, h, nt, None, sl)
+        centre = (n - 1) * h / 2.0
+        yy, xx = np.mgrid[0:n, 0:n].astype(float) * h
+        mask = (np.sqrt((yy - centre) ** 2 + (xx - centre) ** 2)
+                <= geom.radius_m * 0.95).astype(float)
+        bounds = (1.0 / 3500.0 ** 2, 1.0 / 1400.0 ** 2)
+        tw = np.load(os.path.join(HERE, "ring2d_window.npz"))["tw"]
+        out = dict(m_true=m_true, m0=m0, idx=np.asarray(geom.idx, np.int32), wavelet=wav, dt=dt,
+                   h=h, nt=nt, src_list=np.asarray(sl, np.int32), dobs=dobs, sponge=np.zeros(0),
+                   mask=mask, lo=bounds[0], hi=bounds[1], tw=tw)
+        runs = {"gd": dict(n_iter=3),
+                "gcn": dict(n_iter=2, misfit_type="gcn"),
+                "tw": dict(n_iter=2, time_weights=list(tw)),
+                "gn": dict(n_iter=1, optimizer="gauss-newton", n_cg=3)}
+        for key, kw in runs.items():
+            m_rec, hist = fwi.invert(m0, geom, wav, dt, h, nt, dobs, src_list=sl,
+                                     update_mask=mask, m_bounds=bounds, step_frac=0.03, **kw)
+            out["m_" + key] = m_rec
+            out["hist_" + key] = np.asarray(hist)
+        save("invert2d", **out)
 
     # --- 2D sponge (fwi.py:68-69, 313-314) ------------------------------------
     sp = make_sponge((n, n), width=6)
@@ -116,25 +186,27 @@ def main():
                with_cpp=False)
 
     # --- 2D finite aperture (test_gradient_aperture.py) -----------------------
-    fps = build_footprints(geom, width_m=0.003, shape="flat")
-    dobs = fwi.forward_fmc(m_true, geom, wav, dt, h, nt, src_list=[0, 4], footprints=fps)
-    J, g = fwi.misfit_and_gradient(m0, geom, wav, dt, h, nt, dobs, src_list=[0, 4],
-                                   footprints=fps)
-    fp_ptr, fp_idx, fp_w = _fp_csr(fps)
-    save("ring2d_aperture", m_true=m_true, m0=m0, idx=np.asarray(geom.idx, np.int32),
-         wavelet=wav, dt=dt, h=h, nt=nt, src_list=np.asarray([0, 4], np.int32), dobs=dobs,
-         J=J, g=g, fp_ptr=fp_ptr, fp_idx=fp_idx, fp_w=fp_w, sponge=np.zeros(0))
+    if want("ring2d_aperture"):
+        fps = build_footprints(geom, width_m=0.003, shape="flat")
+        dobs = fwi.forward_fmc(m_true, geom, wav, dt, h, nt, src_list=[0, 4], footprints=fps)
+        J, g = fwi.misfit_and_gradient(m0, geom, wav, dt, h, nt, dobs, src_list=[0, 4],
+                                       footprints=fps)
+        fp_ptr, fp_idx, fp_w = _fp_csr(fps)
+        save("ring2d_aperture", m_true=m_true, m0=m0, idx=np.asarray(geom.idx, np.int32),
+             wavelet=wav, dt=dt, h=h, nt=nt, src_list=np.asarray([0, 4], np.int32), dobs=dobs,
+             J=J, g=g, fp_ptr=fp_ptr, fp_idx=fp_idx, fp_w=fp_w, sponge=np.zeros(0))
 
     # --- 2D Gauss-Newton Hv (test_gauss_newton.py) ----------------------------
-    nt_gn = 300
-    wav_gn = ricker(nt_gn, dt, 0.4e6)
-    rng = np.random.default_rng(2)
-    v = rng.standard_normal((n, n))
-    v[:5] = v[-5:] = v[:, :5] = v[:, -5:] = 0.0
-    v *= float(np.mean(m0))
-    Hv = fwi.gn_hessian_vector(m0, geom, wav_gn, dt, h, nt_gn, v, src_list=[0, 4])
-    save("gn2d", m0=m0, idx=np.asarray(geom.idx, np.int32), wavelet=wav_gn, dt=dt, h=h,
-         nt=nt_gn, src_list=np.asarray([0, 4], np.int32), v=v, Hv=Hv, sponge=np.zeros(0))
+    if want("gn2d"):
+        nt_gn = 300
+        wav_gn = ricker(nt_gn, dt, 0.4e6)
+        rng = np.random.default_rng(2)
+        v = rng.standard_normal((n, n))
+        v[:5] = v[-5:] = v[:, :5] = v[:, -5:] = 0.0
+        v *= float(np.mean(m0))
+        Hv = fwi.gn_hessian_vector(m0, geom, wav_gn, dt, h, nt_gn, v, src_list=[0, 4])
+        save("gn2d", m0=m0, idx=np.asarray(geom.idx, np.int32), wavelet=wav_gn, dt=dt, h=h,
+             nt=nt_gn, src_list=np.asarray([0, 4], np.int32), v=v, Hv=Hv, sponge=np.zeros(0))
 
     # --- 3D cylinder, point elements (test_gradient_3d.py) ---------------------
     h3 = 1.5e-3
@@ -147,18 +219,21 @@ def main():
     ct3 = phantom.add_sphere(c3, (0.5, 0.5, 0.5), 0.004, 2700.0, h3)
     point_case("cyl3d_point", cyl, phantom.velocity_to_m(ct3), phantom.velocity_to_m(c3),
                wav3, dt3, h3, nt3, [0, 6])
+    window_case("cyl3d_window", cyl, phantom.velocity_to_m(ct3), phantom.velocity_to_m(c3),
+                wav3, dt3, h3, nt3, [0, 6], 1480.0, 0.35e6, 1.5)
 
     # --- 3D finite aperture (rect footprints) ---------------------------------
-    fps3 = build_footprints(cyl, width_m=0.004, shape="rect", height_m=0.003)
-    mt3, m03 = phantom.velocity_to_m(ct3), phantom.velocity_to_m(c3)
-    dobs3 = fwi.forward_fmc(mt3, cyl, wav3, dt3, h3, nt3, src_list=[0, 6], footprints=fps3)
-    J3, g3 = fwi.misfit_and_gradient(m03, cyl, wav3, dt3, h3, nt3, dobs3, src_list=[0, 6],
-                                     footprints=fps3)
-    fp_ptr, fp_idx, fp_w = _fp_csr(fps3)
-    save("cyl3d_aperture", m_true=mt3, m0=m03, idx=np.asarray(cyl.idx, np.int32),
-         wavelet=wav3, dt=dt3, h=h3, nt=nt3, src_list=np.asarray([0, 6], np.int32),
-         dobs=dobs3, J=J3, g=g3, fp_ptr=fp_ptr, fp_idx=fp_idx, fp_w=fp_w,
-         sponge=np.zeros(0))
+    if want("cyl3d_aperture"):
+        fps3 = build_footprints(cyl, width_m=0.004, shape="rect", height_m=0.003)
+        mt3, m03 = phantom.velocity_to_m(ct3), phantom.velocity_to_m(c3)
+        dobs3 = fwi.forward_fmc(mt3, cyl, wav3, dt3, h3, nt3, src_list=[0, 6], footprints=fps3)
+        J3, g3 = fwi.misfit_and_gradient(m03, cyl, wav3, dt3, h3, nt3, dobs3, src_list=[0, 6],
+                                         footprints=fps3)
+        fp_ptr, fp_idx, fp_w = _fp_csr(fps3)
+        save("cyl3d_aperture", m_true=mt3, m0=m03, idx=np.asarray(cyl.idx, np.int32),
+             wavelet=wav3, dt=dt3, h=h3, nt=nt3, src_list=np.asarray([0, 6], np.int32),
+             dobs=dobs3, J=J3, g=g3, fp_ptr=fp_ptr, fp_idx=fp_idx, fp_w=fp_w,
+             sponge=np.zeros(0))
 
     # --- odd, non-square grids with an element on the border -------------------
     rs = np.random.default_rng(7)

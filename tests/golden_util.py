@@ -20,9 +20,10 @@ CASES = ["ring2d_point", "ring2d_sponge", "ring2d_aperture", "cyl3d_point", "cyl
 # and 0.6%): there the FP32 trace noise (~2e-7 of the data) is 1e-4 of the
 # residual and the FP64 adjoint of that residual alone reproduces the observed
 # 3e-3 / 3e-4 gradient error, so their bound is the conditioning, not the
-# kernels (which match the FP32 restatement bit for bit).
+# kernels (which match the FP32 restatement bit for bit).  cyl3d_window is the
+# cyl3d_point problem with a data window and shares its bound.
 TRACE_TOL = {"odd2d": 1e-4, "odd3d": 1e-4}
-GRAD_TOL = {"cyl3d_point": 5e-3, "cyl3d_aperture": 5e-4}
+GRAD_TOL = {"cyl3d_point": 5e-3, "cyl3d_aperture": 5e-4, "cyl3d_window": 5e-3}
 
 
 def trace_tol(name):

@@ -56,3 +56,27 @@ def test_plan_argument_validation_on_host(lib):
                               cell, w, 3, 0, 0, 0, 0)
     assert rc == _lib.USCT_ERR_ARG and b"power of two" in lib.usct_last_error()
     assert lib.usct_version() >= 10000
+
+
+def test_header_constants_match_the_bindings():
+    text = open(HEADER).read()
+    consts = dict(re.findall(r"#define (USCT_[A-Z_]+) \(?([0-9]+)", text))
+    assert int(consts["USCT_SMOOTH_MAX_RADIUS"]) == _lib.SMOOTH_MAX_RADIUS
+    assert int(consts["USCT_DOT_WS_DOUBLES"]) == _lib.DOT_WS_DOUBLES
+
+
+def test_update_kernels_validate_arguments_on_host(lib):
+    dims = (ctypes.c_int * 3)(4, 5, 6)
+    taps = (ctypes.c_double * 70)(*([0.1] * 70))
+    a, b, c = ctypes.c_void_p(4096), ctypes.c_void_p(8192), ctypes.c_void_p(12288)
+    rc = lib.usct_smooth_dev(a, b, c, 3, dims, taps, _lib.SMOOTH_MAX_RADIUS + 1, None)
+    assert rc == _lib.USCT_ERR_ARG and b"radius" in lib.usct_last_error()
+    rc = lib.usct_smooth_dev(a, a, c, 3, dims, taps, 4, None)
+    assert rc == _lib.USCT_ERR_ARG and b"distinct" in lib.usct_last_error()
+    rc = lib.usct_smooth_dev(a, b, b, 3, dims, taps, 4, None)
+    assert rc == _lib.USCT_ERR_ARG and b"distinct" in lib.usct_last_error()
+    rc = lib.usct_smooth_dev(a, b, c, 4, dims, taps, 4, None)
+    assert rc == _lib.USCT_ERR_ARG and b"ndim" in lib.usct_last_error()
+    rc = lib.usct_model_trial_dev(a, 1.0, b, c, None, None, a, 10, None)
+    assert rc == _lib.USCT_ERR_ARG and b"lo and hi" in lib.usct_last_error()
+    assert lib.usct_vec_dot_dev(None, None, 10, a, None) == _lib.USCT_ERR_ARG

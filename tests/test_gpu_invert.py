@@ -1,0 +1,115 @@
+"""The device-resident FWI loop (openusct_gb300.invert) and its update kernels.
+
+* usct_smooth_dev == scipy.ndimage.gaussian_filter bit for bit; the
+  elementwise update kernels == their NumPy expressions bit for bit; max|x|
+  exact; dot/sum within a few ulps of NumPy;
+* invert() on the device == the host restatement of fwi.invert
+  (oracle/invert.py) driven by the same GB300 backend, for steepest descent
+  (L2, GCN, windowed data) and Gauss-Newton: same accepted steps, the same
+  history and model up to the last-bit differences of the device mean/dot;
+* within the FP32 tolerance of the reference's own fwi.invert (invert2d
+  fixture).
+"""
+
+import numpy as np
+import pytest
+
+from golden_util import load, rel_l2
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def cuda():
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    from openusct_gb300 import build
+    build.build()
+    yield
+
+
+def _ops(shape):
+    from openusct_gb300.invert import ModelOps
+    return ModelOps(shape, torch.device("cuda", 0))
+
+
+@pytest.mark.parametrize("shape,sigma", [((61, 61), 1.0), ((24, 31, 19), 1.0), ((5, 40), 2.0),
+                                         ((3, 4, 5), 1.5), ((33, 20, 7), 0.3)])
+def test_smoothing_is_scipy_bit_for_bit(shape, sigma):
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal(shape)
+    ops = _ops(shape)
+    xd = torch.from_numpy(x).cuda()
+    out = ops.empty()
+    ops.smooth(xd, out, sigma)
+    assert np.array_equal(out.cpu().numpy(), gaussian_filter(x, sigma))
+
+
+def test_update_kernels_match_numpy():
+    rng = np.random.default_rng(12)
+    shape = (37, 29, 23)
+    m, d = rng.standard_normal(shape), rng.standard_normal(shape)
+    mask = (rng.random(shape) > 0.3).astype(float)
+    lo, hi = np.full(shape, -0.5), np.full(shape, 0.7)
+    ops = _ops(shape)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()   # noqa: E731
+    out = ops.empty()
+    ops.mul(T(m), T(mask), out)
+    assert np.array_equal(out.cpu().numpy(), m * mask)
+    ops.axpy(T(m), 0.37, T(d), out)
+    assert np.array_equal(out.cpu().numpy(), m + 0.37 * d)
+    ops.axpy(None, -1.0, T(d), out)
+    assert np.array_equal(out.cpu().numpy(), -d)
+    step = 0.123
+    ops.trial(T(m), -step, T(d), T(lo), T(hi), T(mask), out)
+    mt = m + step * (-d)
+    want = np.where(mask > 0, np.clip(mt, lo, hi), mt)
+    assert np.array_equal(out.cpu().numpy(), want)
+    ops.trial(T(m), step, T(d), T(lo), T(hi), None, out)
+    assert np.array_equal(out.cpu().numpy(), np.clip(m + step * d, lo, hi))
+    ops.trial(T(m), step, T(d), None, None, T(mask), out)
+    assert np.array_equal(out.cpu().numpy(), m + step * d)
+    assert ops.absmax(T(d)) == float(np.max(np.abs(d)))
+    assert abs(ops.dot(T(m), T(d)) - float(m.ravel() @ d.ravel())) <= 1e-12 * np.abs(m * d).sum()
+    assert abs(ops.mean(T(m)) - float(np.mean(m))) <= 1e-14 * np.abs(m).mean()
+    # reproducible: a second reduction gives the same bits
+    assert ops.dot(T(m), T(d)) == ops.dot(T(m), T(d))
+
+
+RUNS = {"gd": dict(n_iter=3), "gcn": dict(n_iter=2, misfit_type="gcn"), "tw": dict(n_iter=2),
+        "gn": dict(n_iter=1, optimizer="gauss-newton", n_cg=3)}
+
+
+@pytest.mark.parametrize("key", sorted(RUNS))
+def test_device_invert_equals_host_loop_and_reference(key):
+    import openusct_gb300.backend as gb
+    from openusct_gb300.invert import invert
+    from oracle.invert import invert as host_invert
+    c = load("invert2d")
+    kw = dict(RUNS[key])
+    if key == "tw":
+        kw["time_weights"] = c["tw"]
+    common = dict(src_list=c.src_list, update_mask=c["mask"],
+                  m_bounds=(float(c["lo"]), float(c["hi"])), step_frac=0.03)
+    m, hist = invert(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"], **common, **kw)
+    mh, hh = host_invert(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"], backend=gb,
+                         **common, **kw)
+    assert len(hist) == len(hh)
+    assert np.max(np.abs(np.asarray(hist) - hh) / np.asarray(hh)) < 1e-9
+    assert rel_l2(m - c["m0"], mh - c["m0"]) < 1e-9
+    # the reference's own inversion, within FP32 tolerance
+    ref = c["hist_" + key]
+    assert len(hist) == len(ref)
+    assert np.max(np.abs(np.asarray(hist) - ref) / ref) < 1e-3
+    assert rel_l2(m - c["m0"], c["m_" + key] - c["m0"]) < 1e-3
+
+
+def test_device_invert_keeps_tensors_on_the_device():
+    from openusct_gb300.invert import invert
+    c = load("invert2d")
+    m0 = torch.from_numpy(c["m0"]).cuda()
+    m, hist = invert(m0, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"], src_list=c.src_list,
+                     n_iter=1, update_mask=torch.from_numpy(c["mask"]).cuda())
+    assert isinstance(m, torch.Tensor) and m.is_cuda and m.dtype == torch.float64
+    assert len(hist) == 2 and hist[1] < hist[0]

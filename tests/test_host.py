@@ -67,3 +67,52 @@ def test_batch_choice_respects_budget():
     assert choose_batch(shape, nt, 256, 256, 256, 64, 1, full) == 32
     assert choose_batch(shape, nt, 256, 256, 256, 64, 1, full - 1) == 16
     assert choose_batch((61, 61), 350, 2, 8, 8, 0, 1, 1 << 40) == 2
+
+
+def test_smoothing_taps_are_scipys_gaussian_kernel():
+    """The taps handed to usct_smooth_dev are exactly scipy's: filtering a unit
+    impulse with gaussian_filter1d returns the kernel itself."""
+    from scipy.ndimage import gaussian_filter1d
+    from openusct_gb300.invert import smoothing_taps
+    for sigma in (0.3, 1.0, 1.7, 3.0):
+        t = smoothing_taps(sigma)
+        r = len(t) - 1
+        delta = np.zeros(4 * r + 9)
+        delta[2 * r + 4] = 1.0
+        k = gaussian_filter1d(delta, sigma)
+        assert np.array_equal(k[2 * r + 4:3 * r + 5], t)
+        assert np.array_equal(k[r + 4:2 * r + 5][::-1], t)
+
+
+def test_smoothing_order_reproduces_scipy_bit_for_bit():
+    """The order usct_smooth_dev adds taps in (centre first, then the pairs from
+    the outermost in, 'reflect' extension with period 2n, axes in order)
+    reproduces scipy.ndimage.gaussian_filter exactly, including a radius larger
+    than an axis."""
+    from scipy.ndimage import gaussian_filter
+    from openusct_gb300.invert import smoothing_taps
+
+    def refl(i, n):
+        k = i % (2 * n)
+        return 2 * n - 1 - k if k >= n else k
+
+    def pass_axis(x, axis, t):
+        r = len(t) - 1
+        xm = np.moveaxis(x, axis, -1)
+        out = np.empty_like(xm)
+        n = xm.shape[-1]
+        for i in range(n):
+            acc = xm[..., i] * t[0]
+            for j in range(r, 0, -1):
+                acc = acc + (xm[..., refl(i - j, n)] + xm[..., refl(i + j, n)]) * t[j]
+            out[..., i] = acc
+        return np.moveaxis(out, -1, axis)
+
+    rng = np.random.default_rng(3)
+    for shape, sigma in (((9, 13, 11), 1.0), ((3, 5), 2.0), ((17,), 1.3)):
+        x = rng.standard_normal(shape)
+        t = smoothing_taps(sigma)
+        y = x
+        for ax in range(x.ndim):
+            y = pass_axis(y, ax, t)
+        assert np.array_equal(y, gaussian_filter(x, sigma))

@@ -18,13 +18,17 @@ def test_shard_partitions_every_item_once():
 
 
 def _fake_compute(m, geom, wavelet, dt, h, nt, dobs, sponge, src_list, misfit_type="l2",
-                  footprints=None):
+                  footprints=None, time_weights=None):
     # per-shot contributions that are easy to sum serially
     g = np.zeros(np.shape(m))
     J = 0.0
-    for s, d in zip(src_list, dobs):
+    tws = [None] * len(dobs) if time_weights is None else list(time_weights)
+    assert len(tws) == len(dobs)
+    for s, d, w in zip(src_list, dobs, tws):
         g += (s + 1) * np.arange(g.size, dtype=float).reshape(g.shape) + float(d.sum())
         J += 0.5 * (s + 1) ** 2
+        if w is not None:   # the window must travel with its own transmit
+            J += float(np.sum(w * d))
     return J, g
 
 
@@ -41,7 +45,10 @@ def _worker(rank, world, port, out):
     m = np.ones((3, 4))
     dobs = np.arange(5 * 2 * 5, dtype=float).reshape(5, 2, 5)
     J, g = sh.misfit_and_gradient(m, _Geom(), None, 1.0, 1.0, 2, dobs, compute=_fake_compute)
-    out.put((rank, J, g))
+    tw = [np.full((2, 5), 0.1 * (i + 1)) for i in range(5)]
+    Jw, _ = sh.misfit_and_gradient(m, _Geom(), None, 1.0, 1.0, 2, dobs, time_weights=tw,
+                                   compute=_fake_compute)
+    out.put((rank, J, g, Jw))
     dist.barrier()
     dist.destroy_process_group()
 
@@ -61,6 +68,10 @@ def test_sharded_sum_equals_serial_on_gloo():
         assert p.exitcode == 0
     dobs = np.arange(5 * 2 * 5, dtype=float).reshape(5, 2, 5)
     J0, g0 = _fake_compute(np.ones((3, 4)), _Geom(), None, 1.0, 1.0, 2, dobs, None, range(5))
-    for _, J, g in res:
+    tw = [np.full((2, 5), 0.1 * (i + 1)) for i in range(5)]
+    Jw0, _ = _fake_compute(np.ones((3, 4)), _Geom(), None, 1.0, 1.0, 2, dobs, None, range(5),
+                           time_weights=tw)
+    for _, J, g, Jw in res:
         assert J == pytest.approx(J0)
         assert np.allclose(g, g0)
+        assert Jw == pytest.approx(Jw0)
