@@ -1,6 +1,8 @@
 """Build recipe for the CUDA library ``openusct_gb300/libusct_gb300.so``.
 
-Three translation units, one ``-gencode`` (sm_103a), built in-tree with nvcc.
+One ``-gencode`` (sm_103a), built in-tree with nvcc: the engine, the no-alloc
+entry point, the model-update kernels, and the TMA-ring kernels once per
+shot-channel count; the objects compile in parallel, then link.
 ``-fmad=false`` keeps every multiply-add unfused unless the kernels ask for
 ``__fmaf_rn`` explicitly, which fixes the rounding of the stencil so the CPU
 restatement can reproduce it bit for bit.
@@ -16,9 +18,14 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "libusct_gb300.so")
-SOURCES = ["usct_engine.cu", "usct_noalloc.cu", "usct_invert.cu"]
-DEPS = ["usct_engine.cu", "usct_noalloc.cu", "usct_invert.cu", "usct_kernels.cuh", "usct_plain.cuh",
-        "usct_tma.cuh"]
+# (source, object, extra flags): the TMA-ring kernels are built once per
+# shot-channel count C, each as its own object
+TMA_CHANNELS = (1, 2, 4, 8, 16, 32, 64)
+SOURCES = [("usct_engine.cu", "usct_engine.o", []), ("usct_noalloc.cu", "usct_noalloc.o", []),
+           ("usct_invert.cu", "usct_invert.o", [])] + [
+    ("usct_tma_inst.cu", f"usct_tma_c{c}.o", [f"-DUSCT_TMA_C={c}"]) for c in TMA_CHANNELS]
+DEPS = ["usct_engine.cu", "usct_noalloc.cu", "usct_invert.cu", "usct_tma_inst.cu",
+        "usct_kernels.cuh", "usct_plain.cuh", "usct_tma.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -32,9 +39,10 @@ def nvcc() -> str:
 OBJDIR = os.path.join(PKG, "_build")
 
 
-def compile_command(src: str, obj: str, verbose_ptxas: bool = False) -> list[str]:
+def compile_command(src: str, obj: str, verbose_ptxas: bool = False,
+                    extra: list[str] | None = None) -> list[str]:
     cmd = [nvcc(), ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17",
-           "-Xcompiler", "-fPIC", "-I", os.path.join(REPO, "include"),
+           "-Xcompiler", "-fPIC", "-I", os.path.join(REPO, "include")] + list(extra or []) + [
            "-c", "-o", obj, os.path.join(CSRC, src)]
     if verbose_ptxas:
         cmd.insert(1, "-Xptxas=-v")
@@ -59,13 +67,14 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     The translation units compile in parallel (one nvcc each), then link."""
     if force or not up_to_date():
         os.makedirs(OBJDIR, exist_ok=True)
-        objs = [os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o") for src in SOURCES]
-        procs = [subprocess.Popen(compile_command(src, obj, verbose_ptxas))
-                 for src, obj in zip(SOURCES, objs)]
+        objs = [os.path.join(OBJDIR, obj) for _, obj, _ in SOURCES]
+        cmds = [compile_command(src, o, verbose_ptxas, extra)
+                for (src, _, extra), o in zip(SOURCES, objs)]
+        procs = [subprocess.Popen(c) for c in cmds]
         codes = [p.wait() for p in procs]
-        if any(codes):
-            raise subprocess.CalledProcessError(next(c for c in codes if c),
-                                                compile_command(SOURCES[0], objs[0]))
+        for c, code in zip(cmds, codes):
+            if code:
+                raise subprocess.CalledProcessError(code, c)
         tmp = LIB + ".tmp"
         subprocess.run(link_command(objs, tmp), check=True)
         os.replace(tmp, LIB)

@@ -134,11 +134,7 @@ static bool tile_supported(bool is3d, int txv, int ty) {
 // (boxes of whole rows) the row box must fit 256 elements (tile_x == 32, 3D).
 static void init_tma_attributes();
 
-static bool tma_supported(const usct_plan* p) {
-    const int TXF = 4 * p->txv;
-    if (p->C >= 4) return (TXF >> p->logC) % 4 == 0;
-    return p->ndim == 3 && p->txv == 32;
-}
+static bool tma_supported(const usct_plan* p) { return tma_tile_ok(p->txv, p->C, p->ndim == 3); }
 
 static void free_plan_dev(usct_plan* p) {
     cudaFree(p->d_sptr); cudaFree(p->d_sent); cudaFree(p->d_rptr); cudaFree(p->d_rent);
@@ -696,41 +692,50 @@ static int smem_optin() {
     return v;
 }
 
-template <class K>
-static int prepare_smem(K kernel, size_t smem) {
-    (void)kernel;
+static int check_smem(size_t smem) {
     if (smem > (size_t)smem_optin()) return set_err(USCT_ERR_ARG, "TMA ring needs %zu B of shared memory", smem);
     return USCT_OK;
 }
 
 // Opt every TMA kernel into the device's full dynamic shared memory once, at
 // plan creation (outside any stream capture).
-template <class K>
-static void allow_smem(K kernel) {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin());
-}
 static void init_tma_attributes() {
     static std::once_flag once;
     std::call_once(once, [] {
-        allow_smem(k_forward_tma<32, 4, true, false>);  allow_smem(k_forward_tma<32, 4, true, true>);
-        allow_smem(k_forward_tma<32, 8, true, false>);  allow_smem(k_forward_tma<32, 8, true, true>);
-        allow_smem(k_forward_tma<64, 2, true, false>);  allow_smem(k_forward_tma<64, 2, true, true>);
-        allow_smem(k_forward_tma<64, 4, true, false>);  allow_smem(k_forward_tma<64, 4, true, true>);
-        allow_smem(k_forward_tma<64, 1, false, false>); allow_smem(k_forward_tma<64, 1, false, true>);
-        allow_smem(k_forward_tma<128, 1, false, false>); allow_smem(k_forward_tma<128, 1, false, true>);
-        allow_smem(k_adjoint_tma<32, 4, true>);  allow_smem(k_adjoint_tma<32, 8, true>);
-        allow_smem(k_adjoint_tma<64, 2, true>);  allow_smem(k_adjoint_tma<64, 4, true>);
-        allow_smem(k_adjoint_tma<64, 1, false>); allow_smem(k_adjoint_tma<128, 1, false>);
+        const int b = smem_optin();
+        tma_allow_smem<1>(b);  tma_allow_smem<2>(b);  tma_allow_smem<4>(b);
+        tma_allow_smem<8>(b);  tma_allow_smem<16>(b); tma_allow_smem<32>(b);
+        tma_allow_smem<64>(b);
         cudaGetLastError();
     });
 }
 
-#define USCT_FWD_TMA_CASE(TX, TY_, D3)                                                        \
-    case TX * 1000 + TY_: {                                                                  \
-        auto k = k_forward_tma<TX, TY_, D3, BORN>;                                           \
-        TRY(prepare_smem(k, smem));                                                          \
-        k<<<grid, dim3(TX, TY_), smem, s>>>(a, mp, R, p->d_err);                             \
-    } break;
+// the per-C launchers of usct_tma_inst.cu: 0 = launched, -1 = no kernel
+static int tma_fwd_dispatch(int C, const TmaLaunch& t, const FwdArgs& a, const FwdMaps& mp,
+                            bool born) {
+    switch (C) {
+        case 1: return tma_forward<1>(t, a, mp, born);
+        case 2: return tma_forward<2>(t, a, mp, born);
+        case 4: return tma_forward<4>(t, a, mp, born);
+        case 8: return tma_forward<8>(t, a, mp, born);
+        case 16: return tma_forward<16>(t, a, mp, born);
+        case 32: return tma_forward<32>(t, a, mp, born);
+        case 64: return tma_forward<64>(t, a, mp, born);
+        default: return -1;
+    }
+}
+static int tma_adj_dispatch(int C, const TmaLaunch& t, const AdjArgs& a, const AdjMaps& mp) {
+    switch (C) {
+        case 1: return tma_adjoint<1>(t, a, mp);
+        case 2: return tma_adjoint<2>(t, a, mp);
+        case 4: return tma_adjoint<4>(t, a, mp);
+        case 8: return tma_adjoint<8>(t, a, mp);
+        case 16: return tma_adjoint<16>(t, a, mp);
+        case 32: return tma_adjoint<32>(t, a, mp);
+        case 64: return tma_adjoint<64>(t, a, mp);
+        default: return -1;
+    }
+}
 
 template <bool BORN>
 static int launch_fwd_tma(usct_plan* p, const FwdArgs& a0, cudaStream_t s) {
@@ -750,34 +755,16 @@ static int launch_fwd_tma(usct_plan* p, const FwdArgs& a0, cudaStream_t s) {
     const int R = BORN ? p->stages_born : p->stages_fwd;
     const FwdStage L = fwd_stage(p->txv, p->ty, p->ndim == 3, BORN, p->C, p->logC, a.sp != nullptr);
     const size_t smem = (size_t)R * L.floats * sizeof(float) + (size_t)R * 8 + 16;
-    const dim3 grid(p->ntx_t, p->nty_t, p->nzc);
-    const int key = p->txv * 1000 + p->ty;
-    if (p->ndim == 3) {
-        switch (key) {
-            USCT_FWD_TMA_CASE(32, 4, true)
-            USCT_FWD_TMA_CASE(32, 8, true)
-            USCT_FWD_TMA_CASE(64, 2, true)
-            USCT_FWD_TMA_CASE(64, 4, true)
-            default: return set_err(USCT_ERR_ARG, "no 3D TMA kernel for tile %d", key);
-        }
-    } else {
-        switch (key) {
-            USCT_FWD_TMA_CASE(64, 1, false)
-            USCT_FWD_TMA_CASE(128, 1, false)
-            default: return set_err(USCT_ERR_ARG, "no 2D TMA kernel for tile %d", key);
-        }
-    }
+    TRY(check_smem(smem));
+    const TmaLaunch t{dim3(p->ntx_t, p->nty_t, p->nzc), smem, R, s, p->d_err, p->txv, p->ty,
+                      p->ndim == 3};
+    if (tma_fwd_dispatch(p->C, t, a, mp, BORN) != 0)
+        return set_err(USCT_ERR_ARG, "no %dD TMA kernel for tile %dx%d with %d shot channels",
+                       p->ndim, p->txv, p->ty, p->C);
     ++p->launches;
     CUDA_TRY(cudaGetLastError());
     return USCT_OK;
 }
-
-#define USCT_ADJ_TMA_CASE(TX, TY_, D3)                                                        \
-    case TX * 1000 + TY_: {                                                                  \
-        auto k = k_adjoint_tma<TX, TY_, D3>;                                                 \
-        TRY(prepare_smem(k, smem));                                                          \
-        k<<<grid, dim3(TX, TY_), smem, s>>>(a, mp, R, p->d_err);                             \
-    } break;
 
 static int launch_adj_tma(usct_plan* p, const AdjArgs& a0, cudaStream_t s) {
     AdjArgs a = a0;
@@ -794,23 +781,12 @@ static int launch_adj_tma(usct_plan* p, const AdjArgs& a0, cudaStream_t s) {
     const AdjStage L = adj_stage(p->txv, p->ty, p->ndim == 3, p->C, p->logC, a.sp != nullptr,
                                  a.gacc != nullptr);
     const size_t smem = (size_t)R * L.floats * sizeof(float) + (size_t)R * 8 + 16;
-    const dim3 grid(p->ntx_t, p->nty_t, p->nzc);
-    const int key = p->txv * 1000 + p->ty;
-    if (p->ndim == 3) {
-        switch (key) {
-            USCT_ADJ_TMA_CASE(32, 4, true)
-            USCT_ADJ_TMA_CASE(32, 8, true)
-            USCT_ADJ_TMA_CASE(64, 2, true)
-            USCT_ADJ_TMA_CASE(64, 4, true)
-            default: return set_err(USCT_ERR_ARG, "no 3D TMA kernel for tile %d", key);
-        }
-    } else {
-        switch (key) {
-            USCT_ADJ_TMA_CASE(64, 1, false)
-            USCT_ADJ_TMA_CASE(128, 1, false)
-            default: return set_err(USCT_ERR_ARG, "no 2D TMA kernel for tile %d", key);
-        }
-    }
+    TRY(check_smem(smem));
+    const TmaLaunch t{dim3(p->ntx_t, p->nty_t, p->nzc), smem, R, s, p->d_err, p->txv, p->ty,
+                      p->ndim == 3};
+    if (tma_adj_dispatch(p->C, t, a, mp) != 0)
+        return set_err(USCT_ERR_ARG, "no %dD TMA kernel for tile %dx%d with %d shot channels",
+                       p->ndim, p->txv, p->ty, p->C);
     ++p->launches;
     CUDA_TRY(cudaGetLastError());
     return USCT_OK;

@@ -26,6 +26,18 @@ namespace usct {
 
 constexpr unsigned long long kWaitNs = 250000000ull;   // 250 ms per stage wait
 constexpr int kSpinCap = 1 << 26;                      // backstop on the poll count
+constexpr uint32_t kSuspendNs = 1000000u;              // longest single suspension (1 ms)
+
+// The kernels take the shot-channel count C as a template parameter: every
+// row length, halo width and cell shift is then a constant and the shared
+// memory addresses fold into immediate offsets (a fifth fewer instructions than
+// with C read from the arguments).  A (tile, C) pair has a TMA kernel when a
+// thread's 4 floats never straddle a tile row end: C >= 4 with whole cells per
+// 4-float group, or C < 4 on the 3D 32-wide tiles.
+__host__ __device__ constexpr int ilog2c(int c) { return c >= 64 ? 6 : c >= 32 ? 5 : c >= 16 ? 4 : c >= 8 ? 3 : c >= 4 ? 2 : c >= 2 ? 1 : 0; }
+__host__ __device__ constexpr bool tma_tile_ok(int txv, int c, bool is3d) {
+    return c >= 4 ? (((4 * txv) >> ilog2c(c)) % 4 == 0) : (is3d && txv == 32);
+}
 
 struct FwdMaps {
     CUtensorMap pc, pp, S, sp, dc, dpp, vm;
@@ -100,14 +112,17 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                  "r"(bytes)
                  : "memory");
 }
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+// test the phase of the given parity; a warp whose phase has not completed is
+// suspended by the hardware until it completes (or kSuspendNs passes) instead
+// of spinning on issue slots the computing warps need
+__device__ __forceinline__ bool mbar_wait_suspend(uint64_t* bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}\n"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
         : "memory");
     return ok != 0;
 }
@@ -118,11 +133,11 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 // bounded wait for the stage barrier b to complete the phase of the given parity
 __device__ __forceinline__ bool wait_bar(uint64_t* b, uint32_t parity) {
-    if (mbar_try_wait(b, parity)) return true;
+    if (mbar_wait_suspend(b, parity)) return true;
     const unsigned long long t0 = global_ns();
     for (int it = 1; it < kSpinCap; ++it) {
-        if (mbar_try_wait(b, parity)) return true;
-        if ((it & 255) == 0 && global_ns() - t0 > kWaitNs) return false;
+        if (mbar_wait_suspend(b, parity)) return true;
+        if (global_ns() - t0 > kWaitNs) return false;
     }
     return false;
 }
@@ -206,18 +221,18 @@ __device__ __forceinline__ void put4(float* d, const float4& v) {
 // ---------------------------------------------------------------------------
 // forward step, TMA ring
 // ---------------------------------------------------------------------------
-template <int TXV, int TY, bool IS3D, bool BORN>
+template <int TXV, int TY, bool IS3D, bool BORN, int C>
 __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : ((TXV * TY >= 256) ? 4 : 8)) k_forward_tma(const FwdArgs a, const __grid_constant__ FwdMaps mp,
                                                          const int R, int* err) {
     extern __shared__ __align__(128) float smf[];
     const Geo& g = a.g;
-    const int C = g.C, logC = g.logC;
-    const int HF = C < 4 ? 4 : C;
+    constexpr int logC = ilog2c(C);
+    constexpr int HF = C < 4 ? 4 : C;
     constexpr int HR = IS3D ? 1 : 0;
     constexpr int TXF = 4 * TXV;
     constexpr int ROWS = TY + 2 * HR;
-    const int SR = TXF + 2 * HF;
-    const int cells = TXF >> logC;
+    constexpr int SR = TXF + 2 * HF;
+    constexpr int cells = TXF >> logC;
     const bool has_sp = a.sp != nullptr;
     const FwdStage L = fwd_stage(TXV, TY, IS3D, BORN, C, logC, has_sp);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smf + (size_t)R * L.floats);
@@ -431,19 +446,19 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
 // ---------------------------------------------------------------------------
 // adjoint step, TMA ring
 // ---------------------------------------------------------------------------
-template <int TXV, int TY, bool IS3D>
+template <int TXV, int TY, bool IS3D, int C>
 __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_tma(const AdjArgs a, const __grid_constant__ AdjMaps mp,
                                                          const int R, int* err) {
     extern __shared__ __align__(128) float smf[];
     const Geo& g = a.g;
-    const int C = g.C, logC = g.logC;
-    const int HF = C < 4 ? 4 : C;
+    constexpr int logC = ilog2c(C);
+    constexpr int HF = C < 4 ? 4 : C;
     constexpr int HR = IS3D ? 1 : 0;
     constexpr int TXF = 4 * TXV;
     constexpr int ROWS = TY + 2 * HR;
-    const int SR = TXF + 2 * HF;
-    const int cells = TXF >> logC;
-    const int SH = cells + 8;   // S halo row length (cells)
+    constexpr int SR = TXF + 2 * HF;
+    constexpr int cells = TXF >> logC;
+    constexpr int SH = cells + 8;   // S halo row length (cells)
     const bool has_sp = a.sp != nullptr;
     const bool has_g = a.gacc != nullptr;
     const AdjStage L = adj_stage(TXV, TY, IS3D, C, logC, has_sp, has_g);
@@ -635,5 +650,25 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
         for (int i = (issued > R ? issued - R : 0); i < issued; ++i) (void)wait_stage(bars, i, R);
     }
 }
+
+// ---------------------------------------------------------------------------
+// launchers, one translation unit per C (usct_tma_inst.cu built with
+// -DUSCT_TMA_C=C): 0 = launched, -1 = no kernel for this tile and C
+// ---------------------------------------------------------------------------
+struct TmaLaunch {
+    dim3 grid;
+    size_t smem;
+    int R;
+    cudaStream_t stream;
+    int* err;
+    int txv, ty;
+    bool is3d;
+};
+template <int C>
+int tma_forward(const TmaLaunch& t, const FwdArgs& a, const FwdMaps& mp, bool born);
+template <int C>
+int tma_adjoint(const TmaLaunch& t, const AdjArgs& a, const AdjMaps& mp);
+template <int C>
+void tma_allow_smem(int bytes);
 
 }  // namespace usct
