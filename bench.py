@@ -221,13 +221,123 @@ def run_reference(args, prob, desc_w, mode):
     print(json.dumps(line))
 
 
+TFM_WORKLOAD = ("TFM delay-and-sum envelope image (imaging.tfm), 64-element ring r=16mm, "
+                "64x1500x64 FMC (dt=0.3*0.15mm/1580 m/s), 120x120 pixels over 0.95 r")
+
+
+def bench_tfm(args):
+    """--workload tfm2d: the reference's TFM (imaging.py:27-74) at the C1
+    acquisition size; one step = one envelope image (analytic signal of every
+    trace + the delay-and-sum over all pairs and pixels)."""
+    import numpy as np
+    import torch
+    from openusct_gb300 import _lib, imaging
+    from openusct_gb300.geometry import RingGeometry
+
+    h, n_el, nt, npix = 0.15e-3, 64, 1500, 120
+    ring = RingGeometry(n_el, 0.016, 255 * h, h)
+    dt = 0.3 * h / 1580.0
+    rng = np.random.default_rng(0)
+    data = rng.standard_normal((n_el, nt, n_el))
+
+    class Geom:
+        element_pos = np.asarray(ring.element_positions, np.float64)
+        radius_m = 0.016
+        dim = 2
+
+    class DS:
+        geometry = Geom()
+        tx_elements = np.arange(n_el)
+        nominal_speed_m_s = 1500.0
+        sample_rate_hz = 1.0 / dt
+
+    DS.data = data
+    dev = torch.device("cuda", 0)
+    lib = _lib.load()
+    s = torch.cuda.current_stream()
+    sp = ctypes_void(s.cuda_stream)
+    P = lambda t: ctypes_void(t.data_ptr())  # noqa: E731
+    axes = imaging.image_axes(DS, npix)
+    dd = torch.from_numpy(data).to(dev)
+    taps = torch.from_numpy(imaging.hilbert_taps(nt).astype(np.float32)).to(dev)
+    A = torch.empty((n_el, n_el, nt, 2), dtype=torch.float32, device=dev)
+    txp = torch.from_numpy(Geom.element_pos.copy()).to(dev)
+    ax = torch.from_numpy(np.stack(axes)).to(dev)
+    ore = torch.empty(npix * npix, dtype=torch.float64, device=dev)
+    oim = torch.empty_like(ore)
+    import ctypes
+
+    def step():
+        _lib.check(lib.usct_analytic_dev(P(dd), P(A), n_el, nt, n_el, P(taps), sp))
+        _lib.check(lib.usct_tfm_dev(P(A), n_el, n_el, nt, P(txp), P(txp), 2, P(ax), npix,
+                                    ctypes.c_double(DS.nominal_speed_m_s),
+                                    ctypes.c_double(DS.sample_rate_hz), P(ore), P(oim), sp))
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    with Clocks(0) as clk:
+        ev[0].record(s)
+        for _ in range(args.steps):
+            step()
+        ev[1].record(s)
+        torch.cuda.synchronize()
+    t_ms = ev[0].elapsed_time(ev[1]) / args.steps
+    # the two kernels separately
+    ev[0].record(s)
+    _lib.check(lib.usct_analytic_dev(P(dd), P(A), n_el, nt, n_el, P(taps), sp))
+    ev[1].record(s)
+    step()
+    ev[2].record(s)
+    torch.cuda.synchronize()
+    t_an = ev[0].elapsed_time(ev[1])
+    t_das = ev[1].elapsed_time(ev[2]) - t_an
+    # end to end through imaging.tfm with the host dataset
+    imaging.tfm(DS, npix=npix)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        imaging.tfm(DS, npix=npix)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    cpu = None
+    if not args.no_cpu:
+        import oracle.tfm as otfm
+        t0 = time.perf_counter()
+        otfm.tfm(data, Geom.element_pos, DS.tx_elements, DS.nominal_speed_m_s, DS.sample_rate_hz,
+                 0.016, npix)
+        cs = time.perf_counter() - t0
+        cpu = {"value": 1.0 / cs, "unit": "images/s", "cores": 1, "kind": "port",
+               "sample": "one full image with the reference algorithm (NumPy/scipy FP64)",
+               "seconds": cs}
+    pairs = npix * npix * n_el * n_el
+    line = {"metric": "TFM images/s", "value": 1000.0 / t_ms, "unit": "images/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Gaussian traces; TFM cost does not depend on values)",
+            "config": {"workload": TFM_WORKLOAD, "n_tx": n_el, "n_rx": n_el, "nt": nt,
+                       "npix": npix, "l2": "the 49 MB analytic signal is L2-resident"},
+            "pairs_per_s": pairs / (t_ms / 1000.0),
+            "kernels_ms": {"k_analytic": t_an, "k_tfm": t_das},
+            "analytic_gflops": 2.0 * n_el * n_el * nt * nt / (t_an / 1000.0) / 1e9,
+            "e2e": {"value": 1.0 / e2e_s, "unit": "images/s", "h2d_bytes_per_step": data.nbytes,
+                    "d2h_bytes_per_step": 2 * 8 * npix * npix, "api": "openusct_gb300.imaging.tfm"},
+            "cpu_baseline": cpu, "gpu_launches": 2 * args.steps, "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
+def ctypes_void(v):
+    import ctypes
+    return ctypes.c_void_p(v)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="grad3d", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="grad3d", choices=sorted(WORKLOADS) + ["tfm2d"])
     ap.add_argument("--n", type=int, default=0, help="override the grid size (smaller variants)")
     ap.add_argument("--nt", type=int, default=0, help="override the time levels")
     ap.add_argument("--batch", type=int, default=0)
@@ -242,6 +352,14 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     import numpy as np
     from openusct_gb300 import problems
+
+    if args.workload == "tfm2d":
+        if args.impl == "reference" or rank != 0:
+            return
+        import torch
+        torch.cuda.set_device(0)
+        bench_tfm(args)
+        return
 
     desc_w, build_prob, C0, k0, mode = WORKLOADS[args.workload]
     if args.n or args.nt:

@@ -312,6 +312,31 @@ int usct_vec_absmax_dev(const double* x, size_t n, double* out, void* stream);
 #define USCT_DOT_WS_DOUBLES 609
 int usct_vec_dot_dev(const double* x, const double* y, size_t n, double* ws, void* stream);
 
+/* ---- total focusing method (delay-and-sum imaging, imaging.py:27-74) ---- */
+/*
+ * Analytic signal of every trace of an FMC (scipy.signal.hilbert along time,
+ * imaging.py:63), written as x + i (x (*) g): a circular convolution with taps
+ * g (device FP32, nt values: the imaginary part of the inverse DFT of scipy's
+ * spectral multiplier, computed by the caller).  data: device FP64
+ * [n_tx][nt][n_rx] (the Dataset layout); analytic: device FP32 interleaved
+ * (re, im) [n_tx][n_rx][nt], trace-major.
+ */
+int usct_analytic_dev(const double* data, float* analytic, int n_tx, int nt, int n_rx,
+                      const float* taps, void* stream);
+/*
+ * TFM image (imaging.py:49-74): for every point r of the C-order grid whose
+ * axis a has coordinates axes[a*npix .. a*npix+npix) (device FP64),
+ * out = sum_{i < n_tx, j < n_rx} analytic[i][j][round((|r - tx_pos[i]| +
+ * |r - rx_pos[j]|) / c * fs)], samples outside [0, nt) skipped; tx_pos
+ * (n_tx x dim) and rx_pos (n_rx x dim) device FP64 element positions; out_re,
+ * out_im device FP64, npix^dim values.  The sample index equals NumPy's
+ * np.round of the same FP64 expression; samples are summed in FP32 over the
+ * receivers of one transmit and in FP64 over the transmits.
+ */
+int usct_tfm_dev(const float* analytic, int n_tx, int n_rx, int nt, const double* tx_pos,
+                 const double* rx_pos, int dim, const double* axes, int npix, double c, double fs,
+                 double* out_re, double* out_im, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,7 +1,8 @@
 """Build recipe for the CUDA library ``openusct_gb300/libusct_gb300.so``.
 
 One ``-gencode`` (sm_103a), built in-tree with nvcc: the engine, the no-alloc
-entry point, the model-update kernels, and the TMA-ring kernels once per
+entry point, the model-update kernels, the TFM imaging kernels, and the
+TMA-ring kernels once per
 shot-channel count; the objects compile in parallel, then link.
 ``-fmad=false`` keeps every multiply-add unfused unless the kernels ask for
 ``__fmaf_rn`` explicitly, which fixes the rounding of the stencil so the CPU
@@ -22,9 +23,9 @@ LIB = os.path.join(PKG, "libusct_gb300.so")
 # shot-channel count C, each as its own object
 TMA_CHANNELS = (1, 2, 4, 8, 16, 32, 64)
 SOURCES = [("usct_engine.cu", "usct_engine.o", []), ("usct_noalloc.cu", "usct_noalloc.o", []),
-           ("usct_invert.cu", "usct_invert.o", [])] + [
+           ("usct_invert.cu", "usct_invert.o", []), ("usct_tfm.cu", "usct_tfm.o", [])] + [
     ("usct_tma_inst.cu", f"usct_tma_c{c}.o", [f"-DUSCT_TMA_C={c}"]) for c in TMA_CHANNELS]
-DEPS = ["usct_engine.cu", "usct_noalloc.cu", "usct_invert.cu", "usct_tma_inst.cu",
+DEPS = ["usct_engine.cu", "usct_noalloc.cu", "usct_invert.cu", "usct_tfm.cu", "usct_tma_inst.cu",
         "usct_kernels.cuh", "usct_plain.cuh", "usct_tma.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -337,9 +337,11 @@ extern "C" int usct_plan_create(usct_plan** out, int ndim, const int* dims, doub
         return ret;
     }
     p->variant = tma_supported(p) ? 1 : 0;
-    // 3D forward sweeps keep six planes in flight (measured best at 192^3 and
-    // 320^3); the 2D rows are short and four suffice
+    // 3D forward sweeps keep six planes in flight and Born sweeps five
+    // (measured best at 192^3 / 320^3, and for the 224^3 Gauss-Newton product);
+    // the 2D rows are short and four (three) suffice
     p->stages_fwd = ndim == 3 ? 6 : 4;
+    p->stages_born = ndim == 3 ? 5 : 3;
     init_tma_attributes();
     *out = p;
     return USCT_OK;

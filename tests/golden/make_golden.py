@@ -26,6 +26,10 @@ own tests:
 * ring2d_window / cyl3d_window -- the ring2d_point / cyl3d_point problems with
                      per-transmit data windows (fwi.py:247-301 time_weights): a
                      tapered mute after the direct arrival, L2 and GCN
+* tfm2d / tfm3d   -- imaging.tfm (imaging.py:27-74): the reference's point-
+                     scatterer dataset of simulation/tests/test_imaging.py:18-38
+                     (16-element ring, scattered field only) and a small 3D
+                     cylinder analogue; envelope and real-part images
 * invert2d        -- fwi.invert (fwi.py:535-660) on the ring2d_point problem
                      with an update mask and bounds as fwi_from_dataset builds
                      them (fwi.py:753-760): 3 steepest-descent iterations (L2),
@@ -74,7 +78,8 @@ def main():
         return not only or name in only
     sys.path.insert(0, os.path.join(args.ref, "simulation"))
     sys.path.insert(0, REPO)
-    from ringfwi import fwi, phantom
+    from ringfwi import fwi, imaging, phantom
+    from ringfwi.acquire import simulate_dataset
     from ringfwi.geometry import CylinderArray, GridArray, RingArray, build_footprints
     from ringfwi.solver import make_sponge
     from ringfwi.sources import ricker
@@ -179,6 +184,38 @@ def main():
             out["m_" + key] = m_rec
             out["hist_" + key] = np.asarray(hist)
         save("invert2d", **out)
+
+    # --- TFM imaging (imaging.py:27-74) -----------------------------------------
+    def tfm_case(name, geom_t, shape, h_t, dt_t, nt_t, f0, centre_frac, radius_scat, npix,
+                 half):
+        if not want(name):
+            return
+        wav_t = ricker(nt_t, dt_t, f0)
+        c_ref = np.full(shape, 1480.0)
+        if len(shape) == 2:
+            c_sc = phantom.add_inclusion(c_ref, centre_frac, radius_scat, 3200.0, h_t)
+        else:
+            c_sc = phantom.add_sphere(c_ref, centre_frac, radius_scat, 3200.0, h_t)
+        ds = simulate_dataset(c_sc, geom_t, wav_t, dt_t, nominal_speed_m_s=1480.0)
+        ds_ref = simulate_dataset(c_ref, geom_t, wav_t, dt_t, nominal_speed_m_s=1480.0)
+        data = ds.data - ds_ref.data
+        ds.data = data
+        img, axes = imaging.tfm(ds, npix=npix, half_size=half)
+        img_re, _ = imaging.tfm(ds, npix=npix, half_size=half, envelope=False)
+        domain = (shape[0] - 1) * h_t
+        true_pos = np.array([f * domain - domain / 2 for f in centre_frac])
+        save(name, data=data, element_pos=ds.geometry.element_pos,
+             tx_elements=np.asarray(ds.tx_elements), c=ds.nominal_speed_m_s,
+             fs=ds.sample_rate_hz, radius_m=ds.geometry.radius_m, npix=npix, half=half,
+             image=img, image_re=img_re, axes=np.stack(axes), true_pos=true_pos)
+
+    ring16 = RingArray(n_elements=16, radius_m=0.020, domain_m=0.050, h=1.0e-3)
+    tfm_case("tfm2d", ring16, (ring16.n, ring16.n), 1.0e-3, 1.5e-7, 320, 0.5e6, (0.62, 0.50),
+             0.003, 81, 0.018)
+    cyl_t = CylinderArray(n_rings=2, per_ring=8, radius_m=0.010, height_m=0.010, domain_m=0.026,
+                          h=1.0e-3)
+    tfm_case("tfm3d", cyl_t, (cyl_t.n,) * 3, 1.0e-3, 1.5e-7, 220, 0.5e6, (0.5, 0.6, 0.45), 0.002,
+             21, 0.008)
 
     # --- 2D sponge (fwi.py:68-69, 313-314) ------------------------------------
     sp = make_sponge((n, n), width=6)

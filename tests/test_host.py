@@ -116,3 +116,44 @@ def test_smoothing_order_reproduces_scipy_bit_for_bit():
         for ax in range(x.ndim):
             y = pass_axis(y, ax, t)
         assert np.array_equal(y, gaussian_filter(x, sigma))
+
+
+def test_hilbert_taps_reproduce_scipy_hilbert():
+    """x + i (x circularly convolved with hilbert_taps) == scipy.signal.hilbert,
+    for even and odd lengths (the identity usct_analytic_dev computes)."""
+    from scipy.signal import hilbert
+    from openusct_gb300.imaging import hilbert_taps
+    rng = np.random.default_rng(5)
+    for nt in (64, 97, 320, 1501):
+        x = rng.standard_normal(nt)
+        g = hilbert_taps(nt)
+        idx = (np.arange(nt)[:, None] - np.arange(nt)[None, :]) % nt
+        y = (g[idx] * x[None, :]).sum(axis=1)
+        a = hilbert(x)
+        assert np.allclose(a.real, x, atol=1e-12)
+        assert np.allclose(a.imag, y, atol=1e-12 * np.abs(x).max() * nt)
+
+
+def test_tfm_fp32_index_margin_holds():
+    """k_tfm decides a sample index in FP32, (d_tx + d_rx) * (fs / c), and
+    falls back to the reference's FP64 expression within 1e-6 * v + 1e-5 of a
+    half-integer.  On ring geometries the FP32 value stays within 2e-7 * v of
+    the FP64 one, so outside the margin both round to the same index."""
+    rng = np.random.default_rng(1)
+    for c, dt, R, npix in ((1480.0, 1.5e-7, 0.02, 61), (1500.0, 0.3 * 0.15e-3 / 1580, 0.016, 80)):
+        fs = 1.0 / dt
+        ang = rng.uniform(0, 2 * np.pi, 48)
+        epos = np.stack([R * np.cos(ang), R * np.sin(ang)], 1)
+        ax = np.linspace(-0.95 * R, 0.95 * R, npix)
+        X, Y = np.meshgrid(ax, ax, indexing="ij")
+        pts = np.stack([X.ravel(), Y.ravel()], 1)
+        d = np.sqrt(((pts[:, None, :] - epos[None, :, :]) ** 2).sum(axis=2))
+        d32 = d.astype(np.float32)
+        rate = np.float32(fs / c)
+        for i in range(0, 48, 5):
+            v64 = ((d[:, i][:, None] + d) / c) * fs
+            v = (d32[:, i][:, None] + d32) * rate
+            assert np.all(np.abs(v.astype(np.float64) - v64) <= 2e-7 * v64 + 1e-9)
+            fr = v - np.floor(v)
+            outside = np.abs(fr - np.float32(0.5)) > np.float32(1e-6) * v + np.float32(1e-5)
+            assert np.array_equal(np.rint(v)[outside].astype(np.float64), np.round(v64)[outside])

@@ -10,11 +10,13 @@
   test_gradient_misfits.py patterns) hold for the oracle.
 """
 
+import os
+
 import numpy as np
 import pytest
 
 import oracle
-from golden_util import CASES, grad_tol, load, rel_l2, rel_max, trace_tol
+from golden_util import CASES, GOLDEN, grad_tol, load, rel_l2, rel_max, trace_tol
 
 POINT_CPP = ["ring2d_point", "cyl3d_point", "odd2d", "odd3d", "parity2d", "parity3d", "gpu3d"]
 
@@ -259,3 +261,18 @@ def test_invert_restatement_matches_reference(key):
     assert len(hist) == len(ref)
     assert np.max(np.abs(np.asarray(hist) - ref) / ref) < 1e-12
     assert rel_l2(m - c["m0"], c["m_" + key] - c["m0"]) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["tfm2d", "tfm3d"])
+def test_tfm_restatement_is_the_reference(name):
+    """oracle.tfm (imaging.py:27-74 restated) reproduces the reference's TFM
+    images bit for bit (envelope and real part)."""
+    from oracle.tfm import tfm
+    z = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    args = (z["data"], z["element_pos"], z["tx_elements"], float(z["c"]), float(z["fs"]),
+            float(z["radius_m"]), int(z["npix"]), float(z["half"]))
+    img, axes = tfm(*args)
+    assert np.array_equal(img, z["image"])
+    assert np.array_equal(np.stack(axes), z["axes"])
+    img_re, _ = tfm(*args, envelope=False)
+    assert np.array_equal(img_re, z["image_re"])
