@@ -35,14 +35,18 @@ def image_axes(dataset, npix, half_size=None):
 def hilbert_taps(nt):
     """g with hilbert(x) = x + i (x circularly convolved with g): the imaginary
     part of the inverse DFT of scipy.signal.hilbert's multiplier h (1 at DC and,
-    for even nt, at Nyquist; 2 on the positive frequencies; 0 on the negative)."""
-    h = np.zeros(nt)
+    for even nt, at Nyquist; 2 on the positive frequencies; 0 on the negative).
+    For even nt that is (2/nt) cot(pi n / nt) at odd n and exactly 0 at even n
+    (the analytic-signal kernel skips the zeros)."""
     if nt % 2 == 0:
-        h[0] = h[nt // 2] = 1.0
-        h[1:nt // 2] = 2.0
-    else:
-        h[0] = 1.0
-        h[1:(nt + 1) // 2] = 2.0
+        n = np.arange(nt)
+        g = np.zeros(nt)
+        odd = n % 2 == 1
+        g[odd] = 2.0 / nt / np.tan(np.pi * n[odd] / nt)
+        return g
+    h = np.zeros(nt)
+    h[0] = 1.0
+    h[1:(nt + 1) // 2] = 2.0
     return np.ascontiguousarray(np.fft.ifft(h).imag)
 
 
