@@ -33,7 +33,7 @@ import torch
 
 from . import _lib
 
-__all__ = ["invert", "smoothing_taps", "ModelOps"]
+__all__ = ["invert", "fwi_from_dataset", "register", "smoothing_taps", "ModelOps"]
 
 
 def smoothing_taps(sigma, truncate=4.0):
@@ -298,3 +298,57 @@ def _gauss_newton(be, ops, m0, geom, wavelet, dt, h, nt, dobs, sponge, src_list,
     history.append(be.misfit(m, geom, wavelet, dt, h, nt, dobs, sponge, src_list, "l2",
                              footprints))
     return m, history
+
+
+def fwi_from_dataset(dataset, start_c=None, update_frac=0.95, m_bounds=None, n_iter=12,
+                     step_frac=0.03, verbose=False, **invert_kw):
+    """FWI of a portable Dataset on the device (fwi.py:702-775, the reference's
+    ``"fwi"`` plugin): the reconstruction grid from the dataset's ground truth
+    (or from the wavelength), element positions mapped to grid indices, a
+    homogeneous or given start model, a radial update mask within
+    ``update_frac`` of the array radius, then :func:`invert`.
+
+    Returns the reference's dict: ``c`` (recovered velocity), ``history``,
+    ``extent``, ``h``, ``geom``.
+    """
+    from .geometry import IndexGeometry
+    ds = dataset
+    dim = int(ds.geometry.dim)
+    if ds.ground_truth is not None:
+        h = ds.ground_truth["h_m"]
+        shape = np.shape(ds.ground_truth["c"])
+    else:
+        ppw = 5.0
+        h = ds.nominal_speed_m_s / (ds.tx_centre_freq_hz * ppw)
+        npix = int(round(2.2 * ds.geometry.radius_m / h)) + 1
+        shape = (npix,) * dim
+    n = shape[0]
+    domain = (n - 1) * h
+    abspos = np.asarray(ds.geometry.element_pos) + domain / 2.0
+    idx = [tuple(int(round(p[a] / h)) for a in reversed(range(dim))) for p in abspos]
+    geom = IndexGeometry(idx)
+    if start_c is None:
+        start_c = np.full(shape, ds.nominal_speed_m_s)
+    start_c = np.asarray(start_c, np.float64)
+    m0 = 1.0 / (start_c * start_c)
+    centre = domain / 2.0
+    coords = np.mgrid[tuple(slice(0, n) for _ in range(dim))].astype(float) * h
+    # transverse radius: both axes in 2D, axes (1, 2) in 3D (the array axis is z)
+    transverse = range(dim) if dim == 2 else range(1, dim)
+    r = np.sqrt(sum((coords[a] - centre) ** 2 for a in transverse))
+    update_mask = (r <= ds.geometry.radius_m * update_frac).astype(float)
+    m_rec, history = invert(m0, geom, ds.tx_wavelet, 1.0 / ds.sample_rate_hz, h,
+                            int(np.shape(ds.data)[1]), ds.data,
+                            src_list=[int(e) for e in ds.tx_elements], n_iter=n_iter,
+                            step_frac=step_frac, update_mask=update_mask, m_bounds=m_bounds,
+                            verbose=verbose, **invert_kw)
+    return {"c": 1.0 / np.sqrt(m_rec), "history": history, "extent": (-centre, domain - centre),
+            "h": h, "geom": geom}
+
+
+def register(plugins):
+    """Install :func:`fwi_from_dataset` as the reference plugin registry's
+    ``"fwi"`` entry (plugins.py:62-66)."""
+    plugins.register("fwi", description="Adjoint-state FWI on the GB300 (sound-speed model)",
+                     output="model")(fwi_from_dataset)
+    return fwi_from_dataset

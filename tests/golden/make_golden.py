@@ -30,6 +30,11 @@ own tests:
                      scatterer dataset of simulation/tests/test_imaging.py:18-38
                      (16-element ring, scattered field only) and a small 3D
                      cylinder analogue; envelope and real-part images
+* gn_vs_gd2d      -- simulation/tests/test_gauss_newton.py:54-75: 4 gradient-
+                     descent and 4 Gauss-Newton iterations (n_cg 8) of fwi.invert
+* pipeline2d      -- simulation/tests/test_pipeline.py:23-59 without the HDF5
+                     round trip (no h5py): simulate_dataset, then the "fwi"
+                     plugin (fwi_from_dataset) from the flaw-free background
 * invert2d        -- fwi.invert (fwi.py:535-660) on the ring2d_point problem
                      with an update mask and bounds as fwi_from_dataset builds
                      them (fwi.py:753-760): 3 steepest-descent iterations (L2),
@@ -78,7 +83,7 @@ def main():
         return not only or name in only
     sys.path.insert(0, os.path.join(args.ref, "simulation"))
     sys.path.insert(0, REPO)
-    from ringfwi import fwi, imaging, phantom
+    from ringfwi import fwi, imaging, phantom, plugins
     from ringfwi.acquire import simulate_dataset
     from ringfwi.geometry import CylinderArray, GridArray, RingArray, build_footprints
     from ringfwi.solver import make_sponge
@@ -160,6 +165,49 @@ def main():
     m_true, m0 = phantom.velocity_to_m(ct), phantom.velocity_to_m(c0)
     point_case("ring2d_point", geom, m_true, m0, wav, dt, h, nt, [0, 4])
     window_case("ring2d_window", geom, m_true, m0, wav, dt, h, nt, [0, 4], 1480.0, 0.4e6, 6.0)
+
+    # --- the reference's Gauss-Newton-vs-descent and pipeline tests ------------
+    if want("gn_vs_gd2d"):
+        h_g = 1.0e-3
+        g_g = RingArray(n_elements=8, radius_m=0.024, domain_m=0.06, h=h_g)
+        n_g = g_g.n
+        dt_g, nt_g = 1.2e-7, 300
+        wav_g = ricker(nt_g, dt_g, 0.4e6)
+        c_t = phantom.coupling_background((n_g, n_g), 3000.0, 1480.0, 0.02, h_g)
+        c_t = phantom.add_inclusion(c_t, (0.55, 0.5), 0.006, 3350.0, h_g)
+        mt_g = phantom.velocity_to_m(c_t)
+        m0_g = phantom.velocity_to_m(phantom.coupling_background((n_g, n_g), 3000.0, 1480.0,
+                                                                   0.02, h_g))
+        sl = [0, 2, 4, 6]
+        dobs_g = fwi.forward_fmc(mt_g, g_g, wav_g, dt_g, h_g, nt_g, src_list=sl)
+        yy, xx = np.mgrid[0:n_g, 0:n_g].astype(float) * h_g
+        cc = (n_g - 1) * h_g / 2
+        mask_g = (np.hypot(xx - cc, yy - cc) <= 0.019).astype(float)
+        m_gd, hist_gd = fwi.invert(m0_g, g_g, wav_g, dt_g, h_g, nt_g, dobs_g, src_list=sl,
+                                   n_iter=4, update_mask=mask_g)
+        m_gn, hist_gn = fwi.invert(m0_g, g_g, wav_g, dt_g, h_g, nt_g, dobs_g, src_list=sl,
+                                   n_iter=4, update_mask=mask_g, optimizer="gauss-newton",
+                                   n_cg=8)
+        save("gn_vs_gd2d", m_true=mt_g, m0=m0_g, idx=np.asarray(g_g.idx, np.int32),
+             wavelet=wav_g, dt=dt_g, h=h_g, nt=nt_g, src_list=np.asarray(sl, np.int32),
+             dobs=dobs_g, sponge=np.zeros(0), mask=mask_g, m_gd=m_gd, hist_gd=np.asarray(hist_gd),
+             m_gn=m_gn, hist_gn=np.asarray(hist_gn))
+    if want("pipeline2d"):
+        h_p = 1.25e-3
+        ring_p = RingArray(n_elements=12, radius_m=0.020, domain_m=0.050, h=h_p)
+        n_p = ring_p.n
+        dt_p, nt_p = 1.2e-7, 360
+        wav_p = ricker(nt_p, dt_p, 0.3e6)
+        c_bg = phantom.coupling_background((n_p, n_p), 3000.0, 1480.0, 0.016, h_p)
+        c_tp = phantom.add_inclusion(c_bg, (0.60, 0.50), 0.005, 2600.0, h_p)
+        ds_p = simulate_dataset(c_tp, ring_p, wav_p, dt_p, nominal_speed_m_s=3000.0)
+        bounds_p = (phantom.velocity_to_m(3600.0), phantom.velocity_to_m(2500.0))
+        res = plugins.run("fwi", ds_p, start_c=c_bg, m_bounds=bounds_p, n_iter=6,
+                          step_frac=0.04)
+        save("pipeline2d", c_true=c_tp, c_bg=c_bg, idx=np.asarray(ring_p.idx, np.int32),
+             element_pos=ds_p.geometry.element_pos, radius_m=ring_p.radius_m, wavelet=wav_p,
+             dt=dt_p, h=h_p, nt=nt_p, data=ds_p.data, lo=bounds_p[0], hi=bounds_p[1],
+             c_rec=res["c"], history=np.asarray(res["history"]), flaw=np.asarray([0.60, 0.50]))
 
     # --- the inversion loops (fwi.py:434-660) ----------------------------------
     if want("invert2d"):

@@ -11,10 +11,12 @@
   fixture).
 """
 
+import os
+
 import numpy as np
 import pytest
 
-from golden_util import load, rel_l2
+from golden_util import GOLDEN, load, rel_l2
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -113,3 +115,111 @@ def test_device_invert_keeps_tensors_on_the_device():
                      n_iter=1, update_mask=torch.from_numpy(c["mask"]).cuda())
     assert isinstance(m, torch.Tensor) and m.is_cuda and m.dtype == torch.float64
     assert len(hist) == 2 and hist[1] < hist[0]
+
+
+def test_gauss_newton_beats_gradient_descent():
+    """simulation/tests/test_gauss_newton.py:54-75 on the device loop: after 4
+    iterations Gauss-Newton (n_cg 8) reduces the misfit more than gradient
+    descent, and below 5 %; the first iterations track the reference's."""
+    from openusct_gb300.invert import invert
+    c = load("gn_vs_gd2d")
+    kw = dict(src_list=c.src_list, n_iter=4, update_mask=c["mask"])
+    _, hist_gd = invert(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"], **kw)
+    _, hist_gn = invert(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                        optimizer="gauss-newton", n_cg=8, **kw)
+    red_gd = hist_gd[-1] / hist_gd[0]
+    red_gn = hist_gn[-1] / hist_gn[0]
+    assert red_gn < red_gd
+    assert red_gn < 0.05
+    assert abs(hist_gd[1] / c["hist_gd"][1] - 1) < 1e-3
+    assert abs(hist_gn[1] / c["hist_gn"][1] - 1) < 1e-2
+
+
+def test_gcn_gradient_matches_finite_differences():
+    """simulation/tests/test_gradient_gcn.py: the device GCN gradient against
+    central differences of the FP64 GCN misfit at the reference's probes."""
+    import oracle
+    import openusct_gb300.backend as gb
+    c = load("ring2d_point")
+    m0 = c["m0"]
+    _, g = gb.misfit_and_gradient(m0, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                                  src_list=c.src_list, misfit_type="gcn")
+    n = m0.shape[0]
+    cc = n // 2
+    for iy, ix in [(cc, cc), (cc + 5, cc), (cc, cc - 6)]:
+        eps = 1e-3 * m0[iy, ix]
+        mp = m0.copy()
+        mp[iy, ix] += eps
+        mm = m0.copy()
+        mm[iy, ix] -= eps
+        Jp = oracle.misfit(mp, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                           src_list=c.src_list, misfit_type="gcn")
+        Jm = oracle.misfit(mm, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                           src_list=c.src_list, misfit_type="gcn")
+        fd = (Jp - Jm) / (2 * eps)
+        ad = g[iy, ix]
+        assert abs(fd - ad) / max(abs(fd), abs(ad), 1e-30) < 0.05
+
+
+def test_time_weights_unit_window_is_identity_and_mute_reduces_misfit():
+    """simulation/tests/test_time_weights.py on the device: unit windows give
+    the unwindowed misfit and gradient bit for bit; a real mute lowers the
+    misfit and changes the gradient."""
+    import openusct_gb300.backend as gb
+    c = load("ring2d_window")
+    args = (c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"])
+    J0, g0 = gb.misfit_and_gradient(*args, src_list=c.src_list)
+    ones = [np.ones((c.nt, len(c["idx"]))) for _ in c.src_list]
+    J1, g1 = gb.misfit_and_gradient(*args, src_list=c.src_list, time_weights=ones)
+    assert J1 == J0 and np.array_equal(g1, g0)
+    J2, g2 = gb.misfit_and_gradient(*args, src_list=c.src_list, time_weights=list(c["tw"]))
+    assert np.isfinite(J2) and np.isfinite(g2).all()
+    assert J2 < J0
+    assert rel_l2(g2, g0) > 1e-2     # (the gradient entries are far below allclose's atol)
+
+
+def test_pipeline_simulate_then_fwi_plugin():
+    """simulation/tests/test_pipeline.py:23-59 without the HDF5 round trip (no
+    h5py): simulate the acquisition with openusct_gb300.acquire, reconstruct it
+    through the "fwi" plugin entry (openusct_gb300.invert.fwi_from_dataset)
+    from the flaw-free background; the misfit halves and the flaw is recovered
+    slower than the background, as the reference's run does (pipeline2d)."""
+    from openusct_gb300.acquire import simulate_dataset
+    from openusct_gb300.geometry import IndexGeometry
+    from openusct_gb300.invert import fwi_from_dataset, register
+    z = np.load(os.path.join(GOLDEN, "pipeline2d.npz"))
+
+    class Ring(IndexGeometry):
+        pass
+
+    ring = Ring([tuple(int(v) for v in r) for r in z["idx"]])
+    ring.h = float(z["h"])
+    ring.radius_m = float(z["radius_m"])
+    ring.element_positions = z["element_pos"]
+    ds = simulate_dataset(z["c_true"], ring, z["wavelet"], float(z["dt"]),
+                          nominal_speed_m_s=3000.0)
+    assert rel_l2(ds.data, z["data"]) < 1e-5
+    res = fwi_from_dataset(ds, start_c=z["c_bg"], m_bounds=(float(z["lo"]), float(z["hi"])),
+                           n_iter=6, step_frac=0.04)
+    hist = res["history"]
+    assert hist[-1] < 0.5 * hist[0]
+    n = res["c"].shape[0]
+    ix, iy = int(round(0.60 * (n - 1))), int(round(0.50 * (n - 1)))
+    assert res["c"][iy, ix] < 2900.0
+    ref = z["history"]
+    assert len(hist) == len(ref)
+    assert abs(hist[0] / ref[0] - 1) < 1e-4
+    assert np.max(np.abs(np.asarray(hist) / ref - 1)) < 1e-2
+
+    class _Registry:
+        entries = {}
+
+        def register(self, name, description="", output="image"):
+            def deco(fn):
+                self.entries[name] = (fn, output)
+                return fn
+            return deco
+
+    reg = _Registry()
+    register(reg)
+    assert reg.entries["fwi"] == (fwi_from_dataset, "model")
