@@ -40,9 +40,9 @@ class FMCProblem:
             batch = choose_batch(self.shape, nt, tx.rows, rx.rows, len(rx.cell), ckpt_k or 0,
                                  _lib.MODE_GRADIENT, int(0.4 * free))
         self.plan = Plan(self.shape, h, dt, nt, tx, rx, batch=batch, ckpt_k=ckpt_k or 0)
-        self.wavelet = torch.as_tensor(np.asarray(wavelet, np.float64)).to(self.device)
-        self.sponge = None if sponge is None else torch.as_tensor(
-            np.asarray(sponge, np.float64)).to(self.device)
+        from .backend import _grid_array, _wavelet
+        self.wavelet = _wavelet(wavelet, nt, self.device)
+        self.sponge = _grid_array(sponge, shape, "sponge", self.device)
         self.keep_bytes = int(0.5 * free) if keep_bytes is None else int(keep_bytes)
         self.n_tx, self.nt, self.n_rx = self.plan.n_tx, self.plan.nt, self.plan.n_rx
 

@@ -224,6 +224,8 @@ def _setup(m, geom, h, dt, nt, src_list, footprints, mode, batch, ckpt_k, tile):
     shape = tuple(np.shape(m))
     if len(shape) not in (2, 3):
         raise ValueError(f"model must be 2D or 3D, got shape {shape}")
+    if int(nt) < 2:
+        raise ValueError(f"nt must be >= 2 (got {nt}): the scheme has no step to take")
     tx, rx = element_csr(geom, shape, src_list, footprints)
     if not batch:
         free, _total = torch.cuda.mem_get_info()
@@ -281,17 +283,59 @@ def _time_weights(time_weights, plan, dev):
     return w.contiguous()
 
 
+def _wavelet(wavelet, nt, dev):
+    """The source series as exactly nt FP64 device samples.  The scheme reads
+    samples 0..nt-2 (fwi.py:65-66 injects series[n-1] for n < nt): fewer than
+    nt-1 is an error, as in the reference; the unused last sample may be
+    missing, extra samples are ignored."""
+    w = _to_dev(wavelet, torch.float64, dev).reshape(-1)
+    nt = int(nt)
+    if w.numel() < nt - 1:
+        raise ValueError(f"the wavelet has {w.numel()} samples; nt = {nt} needs at least {nt - 1}")
+    if w.numel() < nt:
+        w = torch.cat([w, w.new_zeros(nt - w.numel())])
+    return w[:nt].contiguous()
+
+
+def _grid_array(x, shape, name, dev):
+    """A model-shaped FP64 device array (sponge, v), shape-checked."""
+    if x is None:
+        return None
+    t = _to_dev(x, torch.float64, dev)
+    if tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} has shape {tuple(t.shape)}, the model {tuple(shape)}")
+    return t
+
+
+def _no_shots(src_list):
+    """An explicitly empty transmit list: the reference's loops run zero times
+    (fwi.py:113-118, 294-331), so there is nothing to launch."""
+    return src_list is not None and len(list(src_list)) == 0
+
+
+def _zeros(shape, like):
+    if isinstance(like, torch.Tensor) and like.is_cuda:
+        return torch.zeros(shape, dtype=torch.float64, device=like.device)
+    return np.zeros(shape)
+
+
+def _n_receivers(geom, shape, footprints):
+    return len(footprints) if footprints is not None else len(geom.idx)
+
+
 # ---------------------------------------------------------------------------
 # public API (signature-compatible with ringfwi.fwi)
 # ---------------------------------------------------------------------------
 def forward_fmc(m, geom, wavelet, dt, h, nt, sponge=None, src_list=None, footprints=None, *,
                 batch=None, tile=None):
     """Full-matrix capture: data[i, n, j] = receiver j at level n for transmit i."""
+    if _no_shots(src_list):
+        return _zeros((0, int(nt), _n_receivers(geom, np.shape(m), footprints)), m)
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_FORWARD, batch, None, tile)
     dev = torch.device("cuda", torch.cuda.current_device())
     md = _to_dev(m, torch.float64, dev)
-    wd = _to_dev(wavelet, torch.float64, dev)
-    sd = _to_dev(sponge, torch.float64, dev)
+    wd = _wavelet(wavelet, nt, dev)
+    sd = _grid_array(sponge, np.shape(m), "sponge", dev)
     nd = plan.n_tx * plan.nt * plan.n_rx
     # a buffer kept with the plan, so a captured sweep replays into the same place
     dbuf = plan.workspace("traces", 4 * nd, dev)[: 4 * nd].view(torch.float32)
@@ -314,12 +358,15 @@ def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list
     compares dsyn*W with dobs*W and the adjoint source is multiplied by W.
     """
     mt = _check_misfit(misfit_type)
+    if _no_shots(src_list):
+        z = _zeros(np.shape(m), m)
+        return (0.0, z, np.zeros(0)) if return_per_shot else (0.0, z)
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_GRADIENT, batch, ckpt_k,
                   tile)
     dev = torch.device("cuda", torch.cuda.current_device())
     md = _to_dev(m, torch.float64, dev)
-    wd = _to_dev(wavelet, torch.float64, dev)
-    sd = _to_dev(sponge, torch.float64, dev)
+    wd = _wavelet(wavelet, nt, dev)
+    sd = _grid_array(sponge, np.shape(m), "sponge", dev)
     od = _to_dev(dobs, torch.float32, dev)
     if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
         raise ValueError(f"dobs has shape {tuple(od.shape)}, expected "
@@ -346,11 +393,13 @@ def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, misfit
     """Waveform misfit (l2 or gcn) only: one forward sweep per batch (``time_weights``
     as in :func:`misfit_and_gradient`)."""
     mt = _check_misfit(misfit_type)
+    if _no_shots(src_list):
+        return 0.0
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_FORWARD, batch, None, tile)
     dev = torch.device("cuda", torch.cuda.current_device())
     md = _to_dev(m, torch.float64, dev)
-    wd = _to_dev(wavelet, torch.float64, dev)
-    sd = _to_dev(sponge, torch.float64, dev)
+    wd = _wavelet(wavelet, nt, dev)
+    sd = _grid_array(sponge, np.shape(m), "sponge", dev)
     od = _to_dev(dobs, torch.float32, dev)
     if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
         raise ValueError("dobs shape does not match the acquisition")
@@ -381,12 +430,17 @@ def gn_hessian_vector(m, geom, wavelet, dt, h, nt, v, sponge=None, src_list=None
     background is recomputed from checkpoints on the device.
     """
     del wavefields
+    if _no_shots(src_list):
+        z = _zeros(np.shape(m), m)
+        if return_born:
+            return z, _zeros((0, int(nt), _n_receivers(geom, np.shape(m), footprints)), m)
+        return z
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_BORN, batch, ckpt_k, tile)
     dev = torch.device("cuda", torch.cuda.current_device())
     md = _to_dev(m, torch.float64, dev)
-    wd = _to_dev(wavelet, torch.float64, dev)
-    sd = _to_dev(sponge, torch.float64, dev)
-    vd = _to_dev(v, torch.float64, dev)
+    wd = _wavelet(wavelet, nt, dev)
+    sd = _grid_array(sponge, np.shape(m), "sponge", dev)
+    vd = _grid_array(v, np.shape(m), "v", dev)
     hv = torch.empty(plan.shape, dtype=torch.float64, device=dev)
     born = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev) \
         if return_born else None
@@ -416,7 +470,7 @@ def plain_forward_fmc(m, geom, wavelet, dt, h, nt, src_list=None):
     plan = _setup(m, geom, h, dt, nt, src_list, None, _lib.MODE_FORWARD, 1, None, None)
     dev = torch.device("cuda", torch.cuda.current_device())
     md = _to_dev(m, torch.float64, dev)
-    wd = _to_dev(wavelet, torch.float64, dev)
+    wd = _wavelet(wavelet, nt, dev)
     data = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev)
     ws = _workspace(plan.plain_bytes(False), dev)
     _lib.check(plan._lib.usct_plain_forward_fmc_dev(plan.handle, _ptr(md), _ptr(wd), _ptr(data),
@@ -428,8 +482,10 @@ def plain_misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, src_list=None):
     plan = _setup(m, geom, h, dt, nt, src_list, None, _lib.MODE_FORWARD, 1, None, None)
     dev = torch.device("cuda", torch.cuda.current_device())
     md = _to_dev(m, torch.float64, dev)
-    wd = _to_dev(wavelet, torch.float64, dev)
+    wd = _wavelet(wavelet, nt, dev)
     od = _to_dev(dobs, torch.float32, dev)
+    if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
+        raise ValueError("dobs shape does not match the acquisition")
     J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
     g = torch.empty(plan.shape, dtype=torch.float64, device=dev)
     ws = _workspace(plan.plain_bytes(True), dev)

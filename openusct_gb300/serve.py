@@ -128,15 +128,14 @@ class GpuExecutor:
 
     def run(self, req, plan):
         torch = self.torch
-        from .backend import _ptr, _stream
+        from .backend import _grid_array, _ptr, _stream, _wavelet
         lib = plan._lib
         dev = self.device
         st = torch.cuda.Stream(device=dev)
         with torch.cuda.stream(st):
             m = torch.from_numpy(np.ascontiguousarray(req.m, np.float64)).to(dev, non_blocking=True)
-            w = torch.from_numpy(np.ascontiguousarray(req.wavelet, np.float64)).to(dev)
-            sp = None if req.sponge is None else torch.from_numpy(
-                np.ascontiguousarray(req.sponge, np.float64)).to(dev)
+            w = _wavelet(req.wavelet, req.nt, dev)
+            sp = _grid_array(req.sponge, np.shape(req.m), "sponge", dev)
             mws = torch.empty(plan.model_bytes(), dtype=torch.uint8, device=dev)
             s = _stream(st)
             if req.kind == "forward":
@@ -146,6 +145,8 @@ class GpuExecutor:
                                                     _ptr(data), _ptr(mws), _ptr(bws), s))
                 plan.check(st)
                 return {"traces": data.cpu().numpy()}
+            if req.dobs is None or np.shape(req.dobs) != (plan.n_tx, plan.nt, plan.n_rx):
+                raise ValueError(f"dobs must have shape {(plan.n_tx, plan.nt, plan.n_rx)}")
             dobs = torch.from_numpy(np.ascontiguousarray(req.dobs, np.float32)).to(dev)
             bws = torch.empty(plan.batch_bytes(_lib.MODE_GRADIENT), dtype=torch.uint8, device=dev)
             J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)

@@ -157,3 +157,33 @@ def test_tfm_fp32_index_margin_holds():
             fr = v - np.floor(v)
             outside = np.abs(fr - np.float32(0.5)) > np.float32(1e-6) * v + np.float32(1e-5)
             assert np.array_equal(np.rint(v)[outside].astype(np.float64), np.round(v64)[outside])
+
+
+def test_backend_validates_what_the_kernels_would_read():
+    """Arrays the kernels index by the plan's sizes are checked on the host
+    before anything is launched: the wavelet needs nt-1 samples (the last one
+    may be missing, as in the reference), the sponge and v the model's shape,
+    nt >= 2; an empty transmit list returns the reference's empty results."""
+    import torch
+    from openusct_gb300 import backend as gb
+    dev = torch.device("cpu")
+    w = gb._wavelet(np.arange(9.0), 10, dev)
+    assert w.shape == (10,) and float(w[9]) == 0.0 and float(w[8]) == 8.0
+    assert gb._wavelet(np.arange(12.0), 10, dev).shape == (10,)
+    with pytest.raises(ValueError, match="wavelet"):
+        gb._wavelet(np.arange(8.0), 10, dev)
+    with pytest.raises(ValueError, match="sponge"):
+        gb._grid_array(np.ones((4, 5)), (5, 4), "sponge", dev)
+    assert gb._grid_array(None, (5, 4), "sponge", dev) is None
+
+    class G:
+        idx = [(1, 1), (2, 2), (3, 1)]
+    m = np.ones((6, 6))
+    d = gb.forward_fmc(m, G(), np.zeros(5), 1e-7, 1e-3, 5, src_list=[])
+    assert d.shape == (0, 5, 3)
+    J, g = gb.misfit_and_gradient(m, G(), np.zeros(5), 1e-7, 1e-3, 5, np.zeros((0, 5, 3)),
+                                  src_list=[])
+    assert J == 0.0 and np.array_equal(g, np.zeros((6, 6)))
+    assert gb.misfit(m, G(), np.zeros(5), 1e-7, 1e-3, 5, np.zeros((0, 5, 3)), src_list=[]) == 0.0
+    hv = gb.gn_hessian_vector(m, G(), np.zeros(5), 1e-7, 1e-3, 5, np.ones((6, 6)), src_list=[])
+    assert np.array_equal(hv, np.zeros((6, 6)))
