@@ -82,5 +82,17 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     return LIB
 
 
+EXAMPLE = os.path.join(CSRC, "usct_example.cpp")
+
+
+def build_example(out: str) -> str:
+    """Compile the plain C++ example against the library (host compiler only)."""
+    build()
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "c++"
+    subprocess.run([cxx, "-O2", "-std=c++14", "-I", os.path.join(REPO, "include"), EXAMPLE,
+                    "-L", PKG, "-lusct_gb300", f"-Wl,-rpath,{PKG}", "-o", out], check=True)
+    return out
+
+
 if __name__ == "__main__":
     build(force=True, verbose_ptxas=True)

@@ -80,3 +80,10 @@ def test_update_kernels_validate_arguments_on_host(lib):
     rc = lib.usct_model_trial_dev(a, 1.0, b, c, None, None, a, 10, None)
     assert rc == _lib.USCT_ERR_ARG and b"lo and hi" in lib.usct_last_error()
     assert lib.usct_vec_dot_dev(None, None, 10, a, None) == _lib.USCT_ERR_ARG
+
+
+def test_cpp_example_compiles_and_links(tmp_path):
+    """The plain C++ example (usct_example.cpp, the counterpart of the
+    reference's example_main.cpp) builds against the header and library."""
+    exe = build.build_example(str(tmp_path / "usct_example"))
+    assert os.path.exists(exe) and os.access(exe, os.X_OK)

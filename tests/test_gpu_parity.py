@@ -348,3 +348,27 @@ def test_time_weights_shape_is_checked():
     with pytest.raises(ValueError, match="time_weights"):
         gb().misfit_and_gradient(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"], None,
                                  c.src_list, time_weights=c["tw"][:, :-1])
+
+
+def test_cpp_example_against_the_oracle(tmp_path):
+    """Run the plain C++ example (host-pointer C ABI) and check its checksums
+    against the FP64 oracle on the same inputs."""
+    import subprocess
+    from example_inputs import example_problem
+    from openusct_gb300 import build
+    exe = build.build_example(str(tmp_path / "usct_example"))
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    vals = dict(line.split("=") for line in out.splitlines() if "=" in line)
+    vals = {k: float(v) for k, v in vals.items()}
+    assert "usct_example OK" in out
+    p = example_problem()
+    args = (p["wavelet"], p["dt"], p["h"], p["nt"])
+    d = oracle.forward_fmc(p["m_true"], p["idx"], *args)
+    assert abs(vals["forward_sum_abs"] / np.abs(d).sum() - 1) < 1e-5
+    J, g = oracle.misfit_and_gradient(p["m0"], p["idx"], p["wavelet"], p["dt"], p["h"], p["nt"], d)
+    assert abs(vals["l2_J"] / J - 1) < 1e-4
+    assert abs(vals["l2_grad_sum_abs"] / np.abs(g).sum() - 1) < 1e-4
+    Jg, gg = oracle.misfit_and_gradient(p["m0"], p["idx"], p["wavelet"], p["dt"], p["h"],
+                                        p["nt"], d, misfit_type="gcn")
+    assert abs(vals["gcn_J"] / Jg - 1) < 1e-4
+    assert abs(vals["gcn_grad_sum_abs"] / np.abs(gg).sum() - 1) < 1e-4
