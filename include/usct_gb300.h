@@ -336,6 +336,16 @@ int usct_analytic_dev(const double* data, float* analytic, int n_tx, int nt, int
 int usct_tfm_dev(const float* analytic, int n_tx, int n_rx, int nt, const double* tx_pos,
                  const double* rx_pos, int dim, const double* axes, int npix, double c, double fs,
                  double* out_re, double* out_im, void* stream);
+/*
+ * P-arrival mute windows for time_weights (fwi.p_window_weights,
+ * fwi.py:663-699) from the analytic signal of the observed data (as
+ * usct_analytic_dev writes it): per trace the first sample whose envelope
+ * exceeds onset_frac * (max envelope + 1e-30), kept for `keep` samples, then a
+ * cosine roll-off over `taper` samples.  weights: device FP64
+ * [n_tx][nt][n_rx].  The envelope is FP32 (the reference's FP64).
+ */
+int usct_pwindow_dev(const float* analytic, int n_tx, int nt, int n_rx, double onset_frac,
+                     double keep, double taper, double* weights, void* stream);
 
 #ifdef __cplusplus
 }

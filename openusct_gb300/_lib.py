@@ -74,6 +74,7 @@ SIGNATURES = {
     "usct_vec_dot_dev": (_i, [_vp, _vp, ctypes.c_size_t, _vp, _vp]),
     "usct_analytic_dev": (_i, [_vp, _vp, _i, _i, _i, _vp, _vp]),
     "usct_tfm_dev": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _i, _d, _d, _vp, _vp, _vp]),
+    "usct_pwindow_dev": (_i, [_vp, _i, _i, _i, _d, _d, _d, _vp, _vp]),
     "usct_plain_bytes": (ctypes.c_size_t, [_vp, _i]),
     "usct_plain_forward_fmc_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "usct_plain_misfit_and_gradient_dev": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

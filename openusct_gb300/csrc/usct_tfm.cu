@@ -205,7 +205,55 @@ __global__ void __launch_bounds__(kTB) k_tfm(const float2* __restrict__ A, int n
     out_im[p] = sim;
 }
 
+// P-arrival mute windows (fwi.py:663-699): one warp per trace of the
+// trace-major analytic signal; envelope |A| (FP32 hypot), its maximum, the first
+// sample above onset_frac * (max + 1e-30), then the cosine roll-off in FP64,
+// written to W[tx][n][rx] (the time_weights layout).
+__global__ void __launch_bounds__(256) k_pwindow(const float2* __restrict__ A, int n_tx, int nt,
+                                                 int n_rx, double onset_frac, double keep,
+                                                 double taper, double* __restrict__ W) {
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long ntr = (long long)n_tx * n_rx;
+    if (warp >= ntr) return;
+    const float2* tr = A + warp * nt;
+    float mx = 0.f;
+    for (int n = lane; n < nt; n += 32) mx = fmaxf(mx, hypotf(tr[n].x, tr[n].y));
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const double thresh = onset_frac * ((double)mx + 1e-30);
+    int onset = nt;
+    for (int n0 = 0; n0 < nt && onset == nt; n0 += 32) {
+        const int n = n0 + lane;
+        const bool above = n < nt && (double)hypotf(tr[n].x, tr[n].y) > thresh;
+        const unsigned b = __ballot_sync(0xffffffffu, above);
+        if (b) onset = n0 + __ffs(b) - 1;
+    }
+    if (onset == nt) onset = 0;   // np.argmax of an all-false column is 0
+    const long long i = warp / n_rx, j = warp % n_rx;
+    const double end = (double)onset + keep;
+    for (int n = lane; n < nt; n += 32) {
+        double r = (end + taper - (double)n) / taper;
+        r = r < 0.0 ? 0.0 : (r > 1.0 ? 1.0 : r);
+        W[(i * nt + n) * n_rx + j] = 0.5 - 0.5 * cos(3.14159265358979323846 * r);
+    }
+}
+
 }  // namespace
+
+extern "C" int usct_pwindow_dev(const float* analytic, int n_tx, int nt, int n_rx,
+                                double onset_frac, double keep, double taper, double* weights,
+                                void* stream) {
+    if (!analytic || !weights) return usct_internal_error(USCT_ERR_ARG, "null argument");
+    if (n_tx < 1 || nt < 1 || n_rx < 1) return usct_internal_error(USCT_ERR_ARG, "empty data");
+    if (!(taper > 0.0)) return usct_internal_error(USCT_ERR_ARG, "taper must be > 0");
+    const long long threads = (long long)n_tx * n_rx * 32;
+    const long long blocks = (threads + 255) / 256;
+    if (blocks > 0x7fffffffLL) return usct_internal_error(USCT_ERR_ARG, "too many traces");
+    k_pwindow<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const float2*>(analytic), n_tx, nt, n_rx, onset_frac, keep, taper,
+        weights);
+    return cuda_status(cudaGetLastError());
+}
 
 extern "C" int usct_analytic_dev(const double* data, float* analytic, int n_tx, int nt, int n_rx,
                                  const float* taps, void* stream) {

@@ -23,7 +23,8 @@ import torch
 
 from . import _lib
 
-__all__ = ["image_axes", "hilbert_taps", "analytic_signal", "tfm", "register"]
+__all__ = ["image_axes", "hilbert_taps", "analytic_signal", "tfm", "p_window_weights",
+           "register"]
 
 
 def image_axes(dataset, npix, half_size=None):
@@ -116,6 +117,32 @@ def tfm(dataset, npix=120, half_size=None, envelope=True):
     im = out_im.cpu().numpy()
     image = np.hypot(re, im) if envelope else re
     return image.reshape([npix] * dim), axes
+
+
+def p_window_weights(dobs, dt, f0, onset_frac=0.2, keep_cycles=2.5, taper_cycles=0.75,
+                     as_tensor=False):
+    """Per-trace P-arrival mute windows (fwi.p_window_weights, fwi.py:663-699)
+    computed on the device: the onset is the first sample whose envelope
+    exceeds ``onset_frac`` of the trace maximum; the window keeps
+    ``keep_cycles`` of f0 after it and rolls off with a cosine over
+    ``taper_cycles``.  Returns the reference's list of (nt, n_rx) arrays (or
+    one CUDA (n_tx, nt, n_rx) tensor with ``as_tensor``), ready for
+    ``time_weights``."""
+    lib = _lib.load()
+    dev = _dev()
+    A = analytic_signal(dobs)
+    n_tx, n_rx, nt = (int(s) for s in A.shape)
+    keep = keep_cycles / f0 / dt
+    taper = max(1.0, taper_cycles / f0 / dt)
+    W = torch.empty((n_tx, nt, n_rx), dtype=torch.float64, device=dev)
+    st = torch.cuda.current_stream(dev)
+    _lib.check(lib.usct_pwindow_dev(_p(torch.view_as_real(A)), n_tx, nt, n_rx,
+                                    ctypes.c_double(onset_frac), ctypes.c_double(keep),
+                                    ctypes.c_double(taper), _p(W),
+                                    ctypes.c_void_p(st.cuda_stream)))
+    if as_tensor:
+        return W
+    return list(W.cpu().numpy())
 
 
 def register(plugins):

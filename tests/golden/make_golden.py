@@ -26,6 +26,8 @@ own tests:
 * ring2d_window / cyl3d_window -- the ring2d_point / cyl3d_point problems with
                      per-transmit data windows (fwi.py:247-301 time_weights): a
                      tapered mute after the direct arrival, L2 and GCN
+* pwindow2d       -- fwi.p_window_weights (fwi.py:663-699) of the ring2d_point
+                     data (and of the parity2d data, 16 transmits)
 * tfm2d / tfm3d   -- imaging.tfm (imaging.py:27-74): the reference's point-
                      scatterer dataset of simulation/tests/test_imaging.py:18-38
                      (16-element ring, scattered field only) and a small 3D
@@ -165,6 +167,13 @@ def main():
     m_true, m0 = phantom.velocity_to_m(ct), phantom.velocity_to_m(c0)
     point_case("ring2d_point", geom, m_true, m0, wav, dt, h, nt, [0, 4])
     window_case("ring2d_window", geom, m_true, m0, wav, dt, h, nt, [0, 4], 1480.0, 0.4e6, 6.0)
+    if want("pwindow2d"):
+        d_pt = np.load(os.path.join(HERE, "ring2d_point.npz"))["dobs"]
+        d_pa = np.load(os.path.join(HERE, "parity2d.npz"))
+        save("pwindow2d", W_point=np.asarray(fwi.p_window_weights(d_pt, dt, 0.4e6)),
+             dt_point=dt, f0_point=0.4e6,
+             W_parity=np.asarray(fwi.p_window_weights(d_pa["dobs"], float(d_pa["dt"]), 0.3e6)),
+             dt_parity=float(d_pa["dt"]), f0_parity=0.3e6)
 
     # --- the reference's Gauss-Newton-vs-descent and pipeline tests ------------
     if want("gn_vs_gd2d"):
