@@ -14,6 +14,7 @@
 // checkpoints + k stash + 2 adjoint (+2 Born), see usct_batch_bytes.
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -31,6 +32,15 @@
 #include "usct_gb300.h"
 #include "usct_kernels.cuh"
 #include "usct_tma.cuh"
+
+namespace {
+// NVTX range around an entry point (visible in Nsight timelines; a no-op
+// when no tool is attached)
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+};
+}  // namespace
 
 using namespace usct;
 
@@ -901,6 +911,7 @@ static int grid1d(long long n, int bs = 256) {
 extern "C" int usct_model_prepare(usct_plan* p, void* model_ws, const double* m,
                                   const double* sponge, const double* v, const double* wavelet,
                                   void* stream) {
+    Range range_("usct_model_prepare");
     if (!p || !model_ws || !m || !wavelet) return set_err(USCT_ERR_ARG, "null argument");
     cudaStream_t s = (cudaStream_t)stream;
     ModelWS M = carve_model(p, model_ws);
@@ -919,6 +930,7 @@ extern "C" int usct_model_prepare(usct_plan* p, void* model_ws, const double* m,
 
 extern "C" int usct_model_gradient(usct_plan* p, void* model_ws, const double* m, double* grad,
                                    void* stream) {
+    Range range_("usct_model_gradient");
     if (!p || !model_ws || !m || !grad) return set_err(USCT_ERR_ARG, "null argument");
     ModelWS M = carve_model(p, model_ws);
     k_finalize<<<grid1d((long long)p->cells_p), 256, 0, (cudaStream_t)stream>>>(
@@ -984,6 +996,7 @@ static int batch_forward_impl(usct_plan* p, const void* model_ws, void* batch_ws
 
 extern "C" int usct_batch_forward(usct_plan* p, const void* model_ws, void* batch_ws, int b,
                                   int mode, float* traces, void* stream) {
+    Range range_("usct_batch_forward");
     if (!p || !model_ws || !batch_ws) return set_err(USCT_ERR_ARG, "null argument");
     if (b < 0 || b >= p->nbatch) return set_err(USCT_ERR_ARG, "batch %d out of range", b);
     if (mode < USCT_MODE_FORWARD || mode > USCT_MODE_BORN) return set_err(USCT_ERR_ARG, "bad mode");
@@ -1068,6 +1081,7 @@ static int batch_misfit_l2(usct_plan* p, void* batch_ws, int b, const float* dob
 extern "C" int usct_batch_misfit_tw(usct_plan* p, void* batch_ws, int b, const float* dobs,
                                     const float* weights, int misfit_type, double* J,
                                     void* stream) {
+    Range range_("usct_batch_misfit_tw");
     if (!p || !batch_ws || !dobs) return set_err(USCT_ERR_ARG, "null argument");
     if (misfit_type != 0 && misfit_type != 1)
         return set_err(USCT_ERR_ARG, "misfit_type must be 0 (L2) or 1 (GCN)");
@@ -1107,6 +1121,7 @@ extern "C" int usct_batch_adjoint_source(usct_plan* p, void* batch_ws, int b, co
 static int batch_backward_impl(usct_plan* p, void* model_ws, void* batch_ws, int b, cudaStream_t s);
 
 extern "C" int usct_batch_backward(usct_plan* p, void* model_ws, void* batch_ws, int b, void* stream) {
+    Range range_("usct_batch_backward");
     if (!p || !model_ws || !batch_ws) return set_err(USCT_ERR_ARG, "null argument");
     if (b < 0 || b >= p->nbatch) return set_err(USCT_ERR_ARG, "batch %d out of range", b);
     cudaStream_t s = (cudaStream_t)stream;
@@ -1172,6 +1187,7 @@ static int batch_backward_impl(usct_plan* p, void* model_ws, void* batch_ws, int
 extern "C" int usct_forward_fmc_dev(usct_plan* p, const double* m, const double* sponge,
                                     const double* wavelet, float* data, void* model_ws,
                                     void* batch_ws, void* stream) {
+    Range range_("usct_forward_fmc_dev");
     TRY(usct_model_prepare(p, model_ws, m, sponge, nullptr, wavelet, stream));
     for (int b = 0; b < p->nbatch; ++b)
         TRY(usct_batch_forward(p, model_ws, batch_ws, b, USCT_MODE_FORWARD, data, stream));
@@ -1204,6 +1220,7 @@ extern "C" int usct_misfit_and_gradient_tw_dev(usct_plan* p, const double* m, co
                                                const float* weights, int misfit_type, double* J,
                                                double* grad, void* model_ws, void* batch_ws,
                                                void* stream) {
+    Range range_("usct_misfit_and_gradient_tw_dev");
     if (misfit_type != 0 && misfit_type != 1)
         return set_err(USCT_ERR_ARG, "misfit_type must be 0 (L2) or 1 (GCN)");
     TRY(usct_model_prepare(p, model_ws, m, sponge, nullptr, wavelet, stream));
@@ -1219,6 +1236,7 @@ extern "C" int usct_gn_hessian_vector_dev(usct_plan* p, const double* m, const d
                                           const double* wavelet, const double* v, double* hv,
                                           float* born, void* model_ws, void* batch_ws,
                                           void* stream) {
+    Range range_("usct_gn_hessian_vector_dev");
     if (!v) return set_err(USCT_ERR_ARG, "v is null");
     TRY(usct_model_prepare(p, model_ws, m, sponge, v, wavelet, stream));
     for (int b = 0; b < p->nbatch; ++b) {

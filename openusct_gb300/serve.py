@@ -44,10 +44,21 @@ class Request:
     arrival: float = 0.0           # seconds after the stream starts
     rid: int = -1
     batch: int | None = None
+    cancelled: threading.Event = field(default_factory=threading.Event, repr=False)
 
     @property
     def n_shots(self):
         return len(self.src_list) if self.src_list is not None else len(self.geom.idx)
+
+    def cancel(self):
+        """Withdraw the request: if it is still queued it is never admitted;
+        if it is running it stops at the next shot-batch boundary (the device
+        finishes the batch in flight) and its slot and budget are released."""
+        self.cancelled.set()
+
+
+class Cancelled(Exception):
+    """Raised by an executor that stopped a request because it was cancelled."""
 
 
 @dataclass
@@ -68,6 +79,14 @@ class Result:
     @property
     def latency(self):
         return self.t_done - self.t_arrival
+
+    def record(self):
+        """The per-request JSON record (times in seconds from the stream start)."""
+        return {"rid": self.rid, "kind": self.kind, "ok": self.ok, "error": self.error,
+                "shots": self.shots, "device_bytes": self.footprint,
+                "t_arrival": self.t_arrival, "t_admit": self.t_admit, "t_done": self.t_done,
+                "queue_s": max(0.0, self.t_admit - self.t_arrival),
+                "latency_s": self.latency if self.ok else None}
 
 
 @dataclass
@@ -138,11 +157,24 @@ class GpuExecutor:
             sp = _grid_array(req.sponge, np.shape(req.m), "sponge", dev)
             mws = torch.empty(plan.model_bytes(), dtype=torch.uint8, device=dev)
             s = _stream(st)
+            # one shot batch at a time, the request's cancellation checked in
+            # between (the same calls, in the same order, as the whole-acquisition
+            # entry points, so results are identical)
+            def batches():
+                for b in range(plan.nbatch):
+                    if req.cancelled.is_set():
+                        raise Cancelled(f"cancelled after {b} of {plan.nbatch} shot batches")
+                    yield b
+                    st.synchronize()
+
             if req.kind == "forward":
                 bws = torch.empty(plan.batch_bytes(_lib.MODE_FORWARD), dtype=torch.uint8, device=dev)
                 data = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev)
-                _lib.check(lib.usct_forward_fmc_dev(plan.handle, _ptr(m), _ptr(sp), _ptr(w),
-                                                    _ptr(data), _ptr(mws), _ptr(bws), s))
+                _lib.check(lib.usct_model_prepare(plan.handle, _ptr(mws), _ptr(m), _ptr(sp), None,
+                                                  _ptr(w), s))
+                for b in batches():
+                    _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
+                                                      _lib.MODE_FORWARD, _ptr(data), s))
                 plan.check(st)
                 return {"traces": data.cpu().numpy()}
             if req.dobs is None or np.shape(req.dobs) != (plan.n_tx, plan.nt, plan.n_rx):
@@ -151,9 +183,15 @@ class GpuExecutor:
             bws = torch.empty(plan.batch_bytes(_lib.MODE_GRADIENT), dtype=torch.uint8, device=dev)
             J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
             g = torch.empty(plan.shape, dtype=torch.float64, device=dev)
-            _lib.check(lib.usct_misfit_and_gradient_dev(plan.handle, _ptr(m), _ptr(sp), _ptr(w),
-                                                        _ptr(dobs), _ptr(J), _ptr(g), _ptr(mws),
-                                                        _ptr(bws), s))
+            _lib.check(lib.usct_model_prepare(plan.handle, _ptr(mws), _ptr(m), _ptr(sp), None,
+                                              _ptr(w), s))
+            for b in batches():
+                _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
+                                                  _lib.MODE_GRADIENT, None, s))
+                _lib.check(lib.usct_batch_misfit(plan.handle, _ptr(bws), b, _ptr(dobs), _ptr(J),
+                                                 s))
+                _lib.check(lib.usct_batch_backward(plan.handle, _ptr(mws), _ptr(bws), b, s))
+            _lib.check(lib.usct_model_gradient(plan.handle, _ptr(mws), _ptr(m), _ptr(g), s))
             plan.check(st)
             return {"J": float(J.sum().item()), "g": g.cpu().numpy()}
 
@@ -177,6 +215,8 @@ class Engine:
     # -- one request ------------------------------------------------------------
     def _worker(self, req, plan, fp, res, t0, on_done):
         try:
+            if req.cancelled.is_set():
+                raise Cancelled("cancelled before it started")
             out = self.ex.run(req, plan)
             res.ok = True
             res.traces = out.get("traces")
@@ -251,6 +291,13 @@ class Engine:
                 while pending:
                     item = heapq.heappop(pending)
                     _, i, rq, plan, fp = item
+                    if rq.cancelled.is_set():          # withdrawn while queued
+                        res = results[i]
+                        res.error = "Cancelled: withdrawn before admission"
+                        res.t_done = res.t_admit = time.perf_counter() - t0
+                        self.ex.release(plan)
+                        done_count[0] += 1
+                        continue
                     if self.active < self.max_active and self.reserved + fp <= self.budget:
                         self.reserved += fp
                         self.active += 1
@@ -275,6 +322,14 @@ class Engine:
         for th in threads:
             th.join()
         return results
+
+
+def write_records(results, path):
+    """One JSON line per request (Result.record) -- the service's log."""
+    import json
+    with open(path, "w") as f:
+        for r in results:
+            f.write(json.dumps(r.record()) + "\n")
 
 
 def summarize(results, engine=None):

@@ -132,3 +132,37 @@ def test_bounded_wait_reports_and_recovers():
     plan.set("wait_test", 0)
     again = gb.forward_fmc(*args, batch=4, tile=(32, 8, 0, 1))
     assert np.array_equal(again, ref)
+
+
+def test_cancel_mid_flight_then_serve_normally():
+    """A request cancelled while it runs stops at a shot-batch boundary (one
+    shot per batch here, 64 batches), releases its budget and slot, and the
+    next request on the same device is computed exactly as when served alone."""
+    import threading
+    import openusct_gb300.backend as gb
+    from openusct_gb300.geometry import RingGeometry, ricker
+    from openusct_gb300.serve import Engine, GpuExecutor, Request
+    h = 2e-4
+    geom = RingGeometry(64, 0.4 * 127 * h, 127 * h, h)
+    n = geom.n
+    m = np.full((n, n), 1.0 / 1500.0 ** 2)
+    dt = 0.3 * h / 1500.0
+    nt = 600
+    wav = ricker(nt, dt, 1e6)
+    dobs = gb.forward_fmc(m * 0.98, geom, wav, dt, h, nt)
+    long_req = Request(kind="gradient", m=m, geom=geom, wavelet=wav, dt=dt, h=h, nt=nt,
+                       dobs=dobs, batch=1)
+    short = Request(kind="gradient", m=m, geom=geom, wavelet=wav, dt=dt, h=h, nt=nt,
+                    dobs=dobs[[3, 9]], src_list=[3, 9], batch=2, arrival=0.0)
+    eng = Engine(GpuExecutor(), budget_bytes=40 << 30, max_active=1)
+    threading.Timer(0.15, long_req.cancel).start()
+    res = eng.run_stream([long_req], realtime=False)
+    assert not res[0].ok and res[0].error.startswith("Cancelled")
+    k = int(res[0].error.split("after ")[1].split(" of")[0])
+    assert 0 < k < 64
+    assert eng.reserved == 0 and eng.active == 0
+    after = eng.run_stream([short], realtime=False)[0]
+    alone = Engine(GpuExecutor(), budget_bytes=40 << 30, max_active=1).run_stream(
+        [Request(kind="gradient", m=m, geom=geom, wavelet=wav, dt=dt, h=h, nt=nt,
+                 dobs=dobs[[3, 9]], src_list=[3, 9], batch=2)], realtime=False)[0]
+    assert after.ok and after.J == alone.J and np.array_equal(after.g, alone.g)

@@ -109,3 +109,63 @@ def test_percentiles_and_summary():
     assert st.ok == 8 and st.shots == 16
     assert st.p50_s <= st.p99_s
     assert st.shots_per_s > 0
+
+
+class SteppingExecutor(FakeExecutor):
+    """Runs in ten steps and honours cancellation between them, like the GPU
+    executor between shot batches."""
+
+    def __init__(self):
+        super().__init__()
+        self.steps_run = {}
+
+    def run(self, req, plan):
+        from openusct_gb300.serve import Cancelled
+        for k in range(10):
+            if req.cancelled.is_set():
+                raise Cancelled(f"cancelled after {k} of 10 steps")
+            time.sleep(plan.dur / 10)
+            self.steps_run[req.rid] = k + 1
+        return {"J": float(plan.fp)}
+
+
+def test_cancelled_while_queued_is_never_run():
+    ex = SteppingExecutor()
+    eng = Engine(ex, budget_bytes=100, max_active=4)
+    a, b, c = req(80, 0.3, 0.0), req(80, 0.05, 0.01), req(10, 0.05, 0.02)
+    threading.Timer(0.1, b.cancel).start()          # b waits behind a for the budget
+    rs = eng.run_stream([a, b, c])
+    assert rs[0].ok and rs[2].ok
+    assert not rs[1].ok and rs[1].error.startswith("Cancelled")
+    assert 1 not in ex.steps_run
+    assert ex.released == 3 and eng.reserved == 0
+
+
+def test_cancelled_while_running_stops_and_frees_its_budget():
+    ex = SteppingExecutor()
+    eng = Engine(ex, budget_bytes=100, max_active=4)
+    a, b = req(90, 2.0, 0.0), req(90, 0.05, 0.01)
+    threading.Timer(0.3, a.cancel).start()
+    t0 = time.perf_counter()
+    rs = eng.run_stream([a, b])
+    assert time.perf_counter() - t0 < 1.5           # a did not run its 2 s
+    assert not rs[0].ok and rs[0].error.startswith("Cancelled")
+    assert 0 < ex.steps_run.get(0, 0) < 10
+    assert rs[1].ok and rs[1].t_admit >= rs[0].t_done - 1e-3   # b got a's budget afterwards
+    assert eng.reserved == 0 and eng.active == 0
+
+
+def test_per_request_records(tmp_path):
+    import json
+    from openusct_gb300.serve import write_records
+    ex = FakeExecutor()
+    eng = Engine(ex, budget_bytes=100, max_active=2)
+    rs = eng.run_stream([req(40, 0.05, 0.0), req(500, 0.05, 0.0), req(40, 0.05, 0.01)])
+    path = tmp_path / "requests.jsonl"
+    write_records(rs, path)
+    recs = [json.loads(line) for line in path.read_text().splitlines()]
+    assert [r["rid"] for r in recs] == [0, 1, 2]
+    assert recs[0]["ok"] and recs[0]["latency_s"] > 0 and recs[0]["device_bytes"] == 40
+    assert not recs[1]["ok"] and recs[1]["error"].startswith("rejected")
+    assert recs[1]["latency_s"] is None
+    assert all(r["queue_s"] >= 0 for r in recs)
