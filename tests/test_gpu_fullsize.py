@@ -74,3 +74,45 @@ def test_fullsize_batched_equals_one_shot_and_reciprocity(prob):
             tab = d4[a, :, sl[b]]
             tba = d4[b, :, sl[a]]
             assert rel_l2(tab, tba) < 1e-4
+
+
+def test_fullsize_checkpoint_interval_is_bit_exact(prob):
+    """The checkpoint interval k (16, 32, 64 as the gradient configuration
+    sweeps it, and k = nt-1: no recompute at all) changes only what is stored
+    and recomputed, never the result: bit-identical gradients at 192^3."""
+    import openusct_gb300.backend as gb
+    nt = 240
+    wav = _sub(prob, nt)
+    sl = [5, 133]
+    d = gb.forward_fmc(prob.m_true, prob.geom, wav, prob.dt, prob.h, nt, None, sl)
+    ref = None
+    for k in (16, 32, 64, nt - 1):
+        J, g = gb.misfit_and_gradient(prob.m0, prob.geom, wav, prob.dt, prob.h, nt, d,
+                                      src_list=sl, ckpt_k=k)
+        if ref is None:
+            ref = (J, g)
+        else:
+            assert J == ref[0] and np.array_equal(g, ref[1]), k
+
+
+def test_320_grid_traces_and_gradient_vs_fp64():
+    """The large gradient configuration's grid (320^3, dx = 0.12 mm, 16 x 32
+    elements) on a 2-shot subset and a shortened time axis, against the FP64
+    oracle."""
+    import openusct_gb300.backend as gb
+    from openusct_gb300 import problems
+    p = problems.cylinder3d_large(seed=0)
+    nt = 100
+    wav = p.wavelet[:nt]
+    sl = [0, 300]
+    d64 = oracle.forward_fmc(p.m_true, p.geom, wav, p.dt, p.h, nt, None, sl)
+    d32 = gb.forward_fmc(p.m_true, p.geom, wav, p.dt, p.h, nt, None, sl)
+    assert rel_l2(d32, d64) < 1e-5
+    J64, g64 = oracle.misfit_and_gradient(p.m0, p.geom, wav, p.dt, p.h, nt, d64, None, sl, k=20)
+    J32, g32 = gb.misfit_and_gradient(p.m0, p.geom, wav, p.dt, p.h, nt, d64, src_list=sl)
+    assert abs(J32 - J64) <= 1e-4 * J64
+    # after 100 steps the residual is only 4.3e-4 of the data, so the FP32
+    # trace rounding (1.6e-7 of the data, measured with the FP32 restatement)
+    # is 3.6e-4 of the residual: that, not the kernels, bounds the gradient
+    # here (the 192^3 test above holds 1e-4 on a longer time axis)
+    assert rel_l2(g32, g64) < 5e-4

@@ -136,3 +136,30 @@ def test_p_window_weights_match_reference(case, key):
     assert W.shape == Wr.shape
     same = np.all(np.abs(W - Wr) <= 1e-12, axis=1)          # per (transmit, receiver) trace
     assert same.mean() >= 0.98, same.mean()
+
+
+def test_tfm_at_the_c1_acquisition_size_matches_the_oracle():
+    """The C1 acquisition (64-element ring r = 16 mm, 64 x 1500 x 64 FMC,
+    120 x 120 pixels) with seeded data: GPU image against the oracle's
+    restatement of imaging.tfm (which equals the reference bit for bit)."""
+    import oracle.tfm as otfm
+    from openusct_gb300.geometry import RingGeometry
+    from openusct_gb300.imaging import tfm
+    h = 0.15e-3
+    ring = RingGeometry(64, 0.016, 255 * h, h)
+    dt = 0.3 * h / 1580.0
+    rng = np.random.default_rng(0)
+    data = rng.standard_normal((64, 1500, 64))
+    pos = np.asarray(ring.element_positions, np.float64)
+
+    class DS:
+        pass
+    ds = DS()
+    ds.data = data
+    ds.geometry = _Geom(pos, 0.016)
+    ds.tx_elements = np.arange(64)
+    ds.nominal_speed_m_s = 1500.0
+    ds.sample_rate_hz = 1.0 / dt
+    img, _ = tfm(ds, npix=120)
+    ref, _ = otfm.tfm(data, pos, np.arange(64), 1500.0, 1.0 / dt, 0.016, 120)
+    assert rel_l2(img, ref) < 1e-5
