@@ -205,10 +205,33 @@ __device__ __forceinline__ float4 sel4(const bool in[4], const float4& a) {
 }
 // The stencil of usct_kernels.cuh's stencil(), four lanes at once:
 // lap = fma(cen, c, ((x- + x+) [+ (y- + y+)]) + (z- + z+)) * inv_h2, 0 off the interior.
-__device__ __forceinline__ float4 stencil4(const bool in[4], float cen, const float4& c,
-                                           const float4& xm, const float4& xp, const float4& ym,
-                                           const float4& yp, const float4& zm, const float4& zp,
-                                           bool is3d, float inv_h2) {
+// Border lanes (x, y or z on the grid's outer layer) get 0.  The forward
+// kernel tests whether all four lanes are interior -- true on all but the
+// outermost tiles -- and only otherwise builds the per-lane mask (fewer
+// instructions: 2D sweeps 5 % faster); the adjoint keeps the always-masked form
+// below (stencil4m), measured faster there.
+__device__ __forceinline__ float4 stencil4(bool all_in, bool zy_in, const bool x_in[4], float cen,
+                                           const float4& c, const float4& xm, const float4& xp,
+                                           const float4& ym, const float4& yp, const float4& zm,
+                                           const float4& zp, bool is3d, float inv_h2) {
+    float4 t = add4(xm, xp);
+    if (is3d) t = add4(t, add4(ym, yp));
+    t = add4(t, add4(zm, zp));
+    float4 l = mul4(fma4(splat4(cen), c, t), splat4(inv_h2));
+    if (__builtin_expect(!all_in, 0)) {
+        bool in[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) in[q] = zy_in && x_in[q];
+        l = sel4(in, l);
+    }
+    return l;
+}
+// the same with the mask always applied (the adjoint's form: measured faster
+// there than testing for an interior group first)
+__device__ __forceinline__ float4 stencil4m(const bool in[4], float cen, const float4& c,
+                                            const float4& xm, const float4& xp, const float4& ym,
+                                            const float4& yp, const float4& zm, const float4& zp,
+                                            bool is3d, float inv_h2) {
     float4 t = add4(xm, xp);
     if (is3d) t = add4(t, add4(ym, yp));
     t = add4(t, add4(zm, zp));
@@ -259,6 +282,7 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         const int xq = (f + q) >> logC;
         x_in[q] = xq >= 1 && xq <= g.nx - 2;
     }
+    const bool x_all = x_in[0] && x_in[1] && x_in[2] && x_in[3];
     const float cen = IS3D ? -6.f : -4.f;
     const float inv_h2 = g.inv_h2;
     const float wv = a.wav[a.n - 1];
@@ -349,12 +373,10 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         const float4 Sv = cell4s(sm_c + L.o_S + ty * cells, 4 * tx, logC);
         const float4 spv = has_sp ? cell4s(sm_c + L.o_sp + ty * cells, 4 * tx, logC) : f4zero();
         const bool zy_in = y_in && z >= 1 && z <= g.nz - 2;
-        bool in[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) in[q] = zy_in && x_in[q];
+        const bool all_in = zy_in && x_all;
         float lap[4];
-        put4(lap, stencil4(in, cen, cc, xm, xp, ym, yp, cm, cp, IS3D, inv_h2));
-        if (z == snz) {
+        put4(lap, stencil4(all_in, zy_in, x_in, cen, cc, xm, xp, ym, yp, cm, cp, IS3D, inv_h2));
+        if (__builtin_expect(z == snz, 0)) {
             while (si < se) {
                 const SrcEnt e = a.s_ent[si];
                 if (e.z != z) break;
@@ -390,7 +412,7 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
             const float4 dp = ld4(sm_p + L.o_dc + r * SR + col);
             const float4 dppv = ld4(sm_c + L.o_dpp + ty * TXF + 4 * tx);
             const float4 vmv = cell4s(sm_c + L.o_vm + ty * cells, 4 * tx, logC);
-            const float4 dl = stencil4(in, cen, dcc, dxm, dxp, dym, dyp, dm, dp, IS3D, inv_h2);
+            const float4 dl = stencil4(all_in, zy_in, x_in, cen, dcc, dxm, dxp, dym, dyp, dm, dp, IS3D, inv_h2);
             float4 dv = fma4(Sv, dl, fma4(splat4(2.f), dcc, neg4(dppv)));
             dv = fma4(neg4(vmv), make_float4(d2v[0], d2v[1], d2v[2], d2v[3]), dv);
             if (has_sp) dv = mul4(dv, spv);
@@ -407,7 +429,7 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         if (ck_ptr) ck_ptr += g.PP;
         if (d2_ptr) d2_ptr += g.PP;
         if (BORN) dn_ptr += g.PP;
-        if (z == rnz) {
+        if (__builtin_expect(z == rnz, 0)) {
             while (ri < re) {
                 const RxEnt e = a.r_ent[ri];
                 if (e.z != z) break;
@@ -583,7 +605,7 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
 #pragma unroll
         for (int q = 0; q < 4; ++q) in[q] = zy_in && x_in[q];
         // lam^k = (2 lam^{k+1} - lam^{k+2}) + L q, with 2l - l2 as fma(2, l, -l2)
-        const float4 lq = stencil4(in, cen, qc, xm, xp, ym, yp, qm, qp, IS3D, inv_h2);
+        const float4 lq = stencil4m(in, cen, qc, xm, xp, ym, yp, qm, qp, IS3D, inv_h2);
         float4 lk4 = add4(fma4(splat4(2.f), l1c, neg4(l2v)), lq);
         if (has_sp) lk4 = mul4(lk4, spv);
         float lk[4];
