@@ -241,6 +241,78 @@ __device__ __forceinline__ void put4(float* d, const float4& v) {
     d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
 }
 
+// Source injection and receiver sampling for the planes that have entries,
+// out of line: kept as calls, their bodies cannot be predicated into every
+// plane's instruction stream (they run on a few planes of a few tiles).
+struct SrcStep {
+    float4 lap;
+    int si, snz;
+};
+static __device__ __noinline__ SrcStep add_sources(float4 lap4, const SrcEnt* __restrict__ ent, int si,
+                                            int se, int z, int ty, int tx, float wv) {
+    float lap[4] = {lap4.x, lap4.y, lap4.z, lap4.w};
+    while (si < se) {
+        const SrcEnt e = ent[si];
+        if (e.z != z) break;
+        if (e.ly == ty) {
+            const int d = e.f - 4 * tx;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (d == q) lap[q] = lap[q] + e.w * wv;
+        }
+        ++si;
+    }
+    return SrcStep{make_float4(lap[0], lap[1], lap[2], lap[3]), si,
+                   si < se ? ent[si].z : 0x7fffffff};
+}
+struct RxStep {
+    int ri, rnz;
+};
+static __device__ __noinline__ RxStep record_receivers(float4 out4, const RxEnt* __restrict__ ent, int ri,
+                                                int re, int z, int ty, int tx, int C,
+                                                float* __restrict__ rs) {
+    const float out[4] = {out4.x, out4.y, out4.z, out4.w};
+    while (ri < re) {
+        const RxEnt e = ent[ri];
+        if (e.z != z) break;
+        if (e.ly == ty) {
+            const int base = e.lcell * C - 4 * tx;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c = q - base;
+                if (c >= 0 && c < C) rs[(long long)e.slot * C + c] = e.w * out[q];
+            }
+        }
+        ++ri;
+    }
+    return RxStep{ri, ri < re ? ent[ri].z : 0x7fffffff};
+}
+
+// adjoint injection lam^k[rx] -= r^k * w for the planes with receivers
+struct InjStep {
+    float4 lk;
+    int ri, rnz;
+};
+static __device__ __noinline__ InjStep inject_residuals(float4 lk4, const RxEnt* __restrict__ ent,
+                                                       int ri, int re, int z, int ty, int tx, int C,
+                                                       const float* __restrict__ res) {
+    float lk[4] = {lk4.x, lk4.y, lk4.z, lk4.w};
+    while (ri < re) {
+        const RxEnt e = ent[ri];
+        if (e.z != z) break;
+        if (e.ly == ty) {
+            const int base = e.lcell * C - 4 * tx;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c = q - base;
+                if (c >= 0 && c < C) lk[q] = lk[q] - res[(long long)e.j * C + c] * e.w;
+            }
+        }
+        ++ri;
+    }
+    return InjStep{make_float4(lk[0], lk[1], lk[2], lk[3]), ri, ri < re ? ent[ri].z : 0x7fffffff};
+}
+
 // ---------------------------------------------------------------------------
 // forward step, TMA ring
 // ---------------------------------------------------------------------------
@@ -377,18 +449,11 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         float lap[4];
         put4(lap, stencil4(all_in, zy_in, x_in, cen, cc, xm, xp, ym, yp, cm, cp, IS3D, inv_h2));
         if (__builtin_expect(z == snz, 0)) {
-            while (si < se) {
-                const SrcEnt e = a.s_ent[si];
-                if (e.z != z) break;
-                if (e.ly == ty) {
-                    const int d = e.f - 4 * tx;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                        if (d == q) lap[q] = lap[q] + e.w * wv;
-                }
-                ++si;
-            }
-            snz = si < se ? a.s_ent[si].z : 0x7fffffff;
+            const SrcStep st = add_sources(make_float4(lap[0], lap[1], lap[2], lap[3]), a.s_ent,
+                                           si, se, z, ty, tx, wv);
+            put4(lap, st.lap);
+            si = st.si;
+            snz = st.snz;
         }
         // p^n = fma(S, lap, 2c - p^{n-2}) with 2c - p computed as fma(2, c, -p) (2c is exact)
         float4 v4 = fma4(Sv, make_float4(lap[0], lap[1], lap[2], lap[3]),
@@ -430,20 +495,10 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         if (d2_ptr) d2_ptr += g.PP;
         if (BORN) dn_ptr += g.PP;
         if (__builtin_expect(z == rnz, 0)) {
-            while (ri < re) {
-                const RxEnt e = a.r_ent[ri];
-                if (e.z != z) break;
-                if (e.ly == ty) {
-                    const int base = e.lcell * C - 4 * tx;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const int c = q - base;
-                        if (c >= 0 && c < C) a.rs[(long long)e.slot * C + c] = e.w * out[q];
-                    }
-                }
-                ++ri;
-            }
-            rnz = ri < re ? a.r_ent[ri].z : 0x7fffffff;
+            const RxStep st = record_receivers(make_float4(out[0], out[1], out[2], out[3]), a.r_ent,
+                                               ri, re, z, ty, tx, C, a.rs);
+            ri = st.ri;
+            rnz = st.rnz;
         }
 
         // everyone is done with the stage of plane z-1: refill it with plane z-1+R
@@ -611,20 +666,11 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
         float lk[4];
         put4(lk, lk4);
         if (z == rnz) {
-            while (ri < re) {
-                const RxEnt e = a.r_ent[ri];
-                if (e.z != z) break;
-                if (e.ly == ty) {
-                    const int base = e.lcell * C - 4 * tx;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const int c = q - base;
-                        if (c >= 0 && c < C) lk[q] = lk[q] - a.res[(long long)e.j * C + c] * e.w;
-                    }
-                }
-                ++ri;
-            }
-            rnz = ri < re ? a.r_ent[ri].z : 0x7fffffff;
+            const InjStep st = inject_residuals(make_float4(lk[0], lk[1], lk[2], lk[3]), a.r_ent,
+                                                ri, re, z, ty, tx, C, a.res);
+            put4(lk, st.lk);
+            ri = st.ri;
+            rnz = st.rnz;
         }
         if (own) st4(lk_ptr, make_float4(lk[0], lk[1], lk[2], lk[3]));
         lk_ptr += g.PP;
