@@ -17,6 +17,11 @@ oracle's FP64 restatement, bit-identical to the reference C++ core), SM clocks
 sampled during the timed region and the number of kernels launched.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Other workloads (not the default line): --workload ring2d (the 2D 256^2 ring,
+all 64 shots per launch), gn3d (the 224^3 Gauss-Newton Hessian-vector product),
+grad3d_large (320^3, 512 shots, 8 per launch), tfm2d (the TFM image of a
+64 x 1500 x 64 FMC).
 """
 
 from __future__ import annotations
