@@ -23,6 +23,7 @@ or device raises instead of falling back to the CPU.
 from __future__ import annotations
 
 import ctypes
+import threading
 from collections import OrderedDict
 
 import numpy as np
@@ -104,6 +105,7 @@ class Plan:
         if stages is not None:
             self.set("stages", int(stages))
         self._ws = {}
+        self.lock = threading.RLock()
         # launch-bound sizes replay whole batch sweeps as CUDA graphs
         level = int(np.prod(self.shape)) * max(1, self.batch)
         if level <= (1 << 22):
@@ -201,6 +203,7 @@ def choose_batch(shape, nt, n_tx, n_rx, nslot, ckpt_k, mode, budget):
 
 _PLANS: "OrderedDict[tuple, Plan]" = OrderedDict()
 _MAX_PLANS = 8
+_PLANS_LOCK = threading.Lock()
 
 
 def get_plan(shape, h, dt, nt, tx, rx, batch=0, ckpt_k=0, tile_x=0, tile_y=0, zchunk=0,
@@ -208,15 +211,19 @@ def get_plan(shape, h, dt, nt, tx, rx, batch=0, ckpt_k=0, tile_x=0, tile_y=0, zc
     key = (tuple(shape), float(h), float(dt), int(nt), tx.key(), rx.key(), int(batch),
            int(ckpt_k), int(tile_x), int(tile_y), int(zchunk), variant, stages,
            torch.cuda.current_device())
-    p = _PLANS.get(key)
-    if p is None:
-        p = Plan(shape, h, dt, nt, tx, rx, batch, ckpt_k, tile_x, tile_y, zchunk, variant, stages)
-        _PLANS[key] = p
-        while len(_PLANS) > _MAX_PLANS:
-            _PLANS.popitem(last=False)[1].close()
-    else:
-        _PLANS.move_to_end(key)
-    return p
+    with _PLANS_LOCK:
+        p = _PLANS.get(key)
+        if p is None:
+            p = Plan(shape, h, dt, nt, tx, rx, batch, ckpt_k, tile_x, tile_y, zchunk, variant,
+                     stages)
+            _PLANS[key] = p
+            while len(_PLANS) > _MAX_PLANS:
+                # dropped from the cache only: a call still holding it keeps it
+                # alive, and it is destroyed when the last reference goes
+                _PLANS.popitem(last=False)
+        else:
+            _PLANS.move_to_end(key)
+        return p
 
 
 def _setup(m, geom, h, dt, nt, src_list, footprints, mode, batch, ckpt_k, tile):
@@ -332,21 +339,23 @@ def forward_fmc(m, geom, wavelet, dt, h, nt, sponge=None, src_list=None, footpri
     if _no_shots(src_list):
         return _zeros((0, int(nt), _n_receivers(geom, np.shape(m), footprints)), m)
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_FORWARD, batch, None, tile)
-    dev = torch.device("cuda", torch.cuda.current_device())
-    md = _to_dev(m, torch.float64, dev)
-    wd = _wavelet(wavelet, nt, dev)
-    sd = _grid_array(sponge, np.shape(m), "sponge", dev)
-    nd = plan.n_tx * plan.nt * plan.n_rx
-    # a buffer kept with the plan, so a captured sweep replays into the same place
-    dbuf = plan.workspace("traces", 4 * nd, dev)[: 4 * nd].view(torch.float32)
-    mws = plan.workspace("model", plan.model_bytes(), dev)
-    bws = plan.workspace(_lib.MODE_FORWARD, plan.batch_bytes(_lib.MODE_FORWARD), dev)
-    with _on_exec_stream() as st:
-        _lib.check(plan._lib.usct_forward_fmc_dev(plan.handle, _ptr(md), _ptr(sd), _ptr(wd),
-                                                  _ptr(dbuf), _ptr(mws), _ptr(bws), _stream(st)))
-        plan.check(st)
-    data = dbuf.view(plan.n_tx, plan.nt, plan.n_rx).clone()
-    return _out(data, m)
+    with plan.lock:   # one call at a time per plan: its workspaces are shared
+        dev = torch.device("cuda", torch.cuda.current_device())
+        md = _to_dev(m, torch.float64, dev)
+        wd = _wavelet(wavelet, nt, dev)
+        sd = _grid_array(sponge, np.shape(m), "sponge", dev)
+        nd = plan.n_tx * plan.nt * plan.n_rx
+        # a buffer kept with the plan, so a captured sweep replays into the same place
+        dbuf = plan.workspace("traces", 4 * nd, dev)[: 4 * nd].view(torch.float32)
+        mws = plan.workspace("model", plan.model_bytes(), dev)
+        bws = plan.workspace(_lib.MODE_FORWARD, plan.batch_bytes(_lib.MODE_FORWARD), dev)
+        with _on_exec_stream() as st:
+            _lib.check(plan._lib.usct_forward_fmc_dev(plan.handle, _ptr(md), _ptr(sd), _ptr(wd),
+                                                      _ptr(dbuf), _ptr(mws), _ptr(bws), _stream(st)))
+            plan.check(st)
+            with torch.cuda.stream(st):   # copied out before the next call may reuse the buffer
+                data = dbuf.view(plan.n_tx, plan.nt, plan.n_rx).clone()
+        return _out(data, m)
 
 
 def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None,
@@ -363,29 +372,30 @@ def misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list
         return (0.0, z, np.zeros(0)) if return_per_shot else (0.0, z)
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_GRADIENT, batch, ckpt_k,
                   tile)
-    dev = torch.device("cuda", torch.cuda.current_device())
-    md = _to_dev(m, torch.float64, dev)
-    wd = _wavelet(wavelet, nt, dev)
-    sd = _grid_array(sponge, np.shape(m), "sponge", dev)
-    od = _to_dev(dobs, torch.float32, dev)
-    if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
-        raise ValueError(f"dobs has shape {tuple(od.shape)}, expected "
-                         f"{(plan.n_tx, plan.nt, plan.n_rx)}")
-    tw = _time_weights(time_weights, plan, dev)
-    J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
-    g = torch.empty(plan.shape, dtype=torch.float64, device=dev)
-    mws = plan.workspace("model", plan.model_bytes(), dev)
-    bws = plan.workspace(_lib.MODE_GRADIENT, plan.batch_bytes(_lib.MODE_GRADIENT), dev)
-    with _on_exec_stream() as st:
-        _lib.check(plan._lib.usct_misfit_and_gradient_tw_dev(
-            plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(od), _ptr(tw), mt, _ptr(J), _ptr(g),
-            _ptr(mws), _ptr(bws), _stream(st)))
-        plan.check(st)
-    Jh = J.cpu().numpy()
-    Jv = float(np.sum(Jh))
-    if return_per_shot:
-        return Jv, _out(g, m), Jh
-    return Jv, _out(g, m)
+    with plan.lock:   # one call at a time per plan: its workspaces are shared
+        dev = torch.device("cuda", torch.cuda.current_device())
+        md = _to_dev(m, torch.float64, dev)
+        wd = _wavelet(wavelet, nt, dev)
+        sd = _grid_array(sponge, np.shape(m), "sponge", dev)
+        od = _to_dev(dobs, torch.float32, dev)
+        if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
+            raise ValueError(f"dobs has shape {tuple(od.shape)}, expected "
+                             f"{(plan.n_tx, plan.nt, plan.n_rx)}")
+        tw = _time_weights(time_weights, plan, dev)
+        J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
+        g = torch.empty(plan.shape, dtype=torch.float64, device=dev)
+        mws = plan.workspace("model", plan.model_bytes(), dev)
+        bws = plan.workspace(_lib.MODE_GRADIENT, plan.batch_bytes(_lib.MODE_GRADIENT), dev)
+        with _on_exec_stream() as st:
+            _lib.check(plan._lib.usct_misfit_and_gradient_tw_dev(
+                plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(od), _ptr(tw), mt, _ptr(J), _ptr(g),
+                _ptr(mws), _ptr(bws), _stream(st)))
+            plan.check(st)
+        Jh = J.cpu().numpy()
+        Jv = float(np.sum(Jh))
+        if return_per_shot:
+            return Jv, _out(g, m), Jh
+        return Jv, _out(g, m)
 
 
 def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, misfit_type="l2",
@@ -396,29 +406,30 @@ def misfit(m, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, misfit
     if _no_shots(src_list):
         return 0.0
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_FORWARD, batch, None, tile)
-    dev = torch.device("cuda", torch.cuda.current_device())
-    md = _to_dev(m, torch.float64, dev)
-    wd = _wavelet(wavelet, nt, dev)
-    sd = _grid_array(sponge, np.shape(m), "sponge", dev)
-    od = _to_dev(dobs, torch.float32, dev)
-    if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
-        raise ValueError("dobs shape does not match the acquisition")
-    tw = _time_weights(time_weights, plan, dev)
-    J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
-    mws = plan.workspace("model", plan.model_bytes(), dev)
-    bws = plan.workspace(_lib.MODE_FORWARD, plan.batch_bytes(_lib.MODE_FORWARD), dev)
-    lib = plan._lib
-    with _on_exec_stream() as st:
-        s = _stream(st)
-        _lib.check(lib.usct_model_prepare(plan.handle, _ptr(mws), _ptr(md), _ptr(sd), None,
-                                          _ptr(wd), s))
-        for b in range(plan.nbatch):
-            _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
-                                              _lib.MODE_FORWARD, None, s))
-            _lib.check(lib.usct_batch_misfit_tw(plan.handle, _ptr(bws), b, _ptr(od), _ptr(tw),
-                                                mt, _ptr(J), s))
-        plan.check(st)
-    return float(np.sum(J.cpu().numpy()))
+    with plan.lock:   # one call at a time per plan: its workspaces are shared
+        dev = torch.device("cuda", torch.cuda.current_device())
+        md = _to_dev(m, torch.float64, dev)
+        wd = _wavelet(wavelet, nt, dev)
+        sd = _grid_array(sponge, np.shape(m), "sponge", dev)
+        od = _to_dev(dobs, torch.float32, dev)
+        if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
+            raise ValueError("dobs shape does not match the acquisition")
+        tw = _time_weights(time_weights, plan, dev)
+        J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
+        mws = plan.workspace("model", plan.model_bytes(), dev)
+        bws = plan.workspace(_lib.MODE_FORWARD, plan.batch_bytes(_lib.MODE_FORWARD), dev)
+        lib = plan._lib
+        with _on_exec_stream() as st:
+            s = _stream(st)
+            _lib.check(lib.usct_model_prepare(plan.handle, _ptr(mws), _ptr(md), _ptr(sd), None,
+                                              _ptr(wd), s))
+            for b in range(plan.nbatch):
+                _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
+                                                  _lib.MODE_FORWARD, None, s))
+                _lib.check(lib.usct_batch_misfit_tw(plan.handle, _ptr(bws), b, _ptr(od), _ptr(tw),
+                                                    mt, _ptr(J), s))
+            plan.check(st)
+        return float(np.sum(J.cpu().numpy()))
 
 
 def gn_hessian_vector(m, geom, wavelet, dt, h, nt, v, sponge=None, src_list=None,
@@ -436,30 +447,35 @@ def gn_hessian_vector(m, geom, wavelet, dt, h, nt, v, sponge=None, src_list=None
             return z, _zeros((0, int(nt), _n_receivers(geom, np.shape(m), footprints)), m)
         return z
     plan = _setup(m, geom, h, dt, nt, src_list, footprints, _lib.MODE_BORN, batch, ckpt_k, tile)
-    dev = torch.device("cuda", torch.cuda.current_device())
-    md = _to_dev(m, torch.float64, dev)
-    wd = _wavelet(wavelet, nt, dev)
-    sd = _grid_array(sponge, np.shape(m), "sponge", dev)
-    vd = _grid_array(v, np.shape(m), "v", dev)
-    hv = torch.empty(plan.shape, dtype=torch.float64, device=dev)
-    born = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev) \
-        if return_born else None
-    mws = plan.workspace("model", plan.model_bytes(), dev)
-    bws = plan.workspace(_lib.MODE_BORN, plan.batch_bytes(_lib.MODE_BORN), dev)
-    with _on_exec_stream() as st:
-        _lib.check(plan._lib.usct_gn_hessian_vector_dev(
-            plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(vd), _ptr(hv), _ptr(born), _ptr(mws),
-            _ptr(bws), _stream(st)))
-        plan.check(st)
-    if return_born:
-        return _out(hv, m), _out(born, m)
-    return _out(hv, m)
+    with plan.lock:   # one call at a time per plan: its workspaces are shared
+        dev = torch.device("cuda", torch.cuda.current_device())
+        md = _to_dev(m, torch.float64, dev)
+        wd = _wavelet(wavelet, nt, dev)
+        sd = _grid_array(sponge, np.shape(m), "sponge", dev)
+        vd = _grid_array(v, np.shape(m), "v", dev)
+        hv = torch.empty(plan.shape, dtype=torch.float64, device=dev)
+        born = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev) \
+            if return_born else None
+        mws = plan.workspace("model", plan.model_bytes(), dev)
+        bws = plan.workspace(_lib.MODE_BORN, plan.batch_bytes(_lib.MODE_BORN), dev)
+        with _on_exec_stream() as st:
+            _lib.check(plan._lib.usct_gn_hessian_vector_dev(
+                plan.handle, _ptr(md), _ptr(sd), _ptr(wd), _ptr(vd), _ptr(hv), _ptr(born), _ptr(mws),
+                _ptr(bws), _stream(st)))
+            plan.check(st)
+        if return_born:
+            return _out(hv, m), _out(born, m)
+        return _out(hv, m)
 
 
 def release():
-    """Free every cached plan and workspace."""
-    while _PLANS:
-        _PLANS.popitem()[1].close()
+    """Free every cached plan and workspace (waiting for calls in flight)."""
+    with _PLANS_LOCK:
+        plans = list(_PLANS.values())
+        _PLANS.clear()
+    for p in plans:
+        with p.lock:
+            p.close()
     torch.cuda.empty_cache()
 
 
@@ -468,27 +484,29 @@ def release():
 # ---------------------------------------------------------------------------
 def plain_forward_fmc(m, geom, wavelet, dt, h, nt, src_list=None):
     plan = _setup(m, geom, h, dt, nt, src_list, None, _lib.MODE_FORWARD, 1, None, None)
-    dev = torch.device("cuda", torch.cuda.current_device())
-    md = _to_dev(m, torch.float64, dev)
-    wd = _wavelet(wavelet, nt, dev)
-    data = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev)
-    ws = _workspace(plan.plain_bytes(False), dev)
-    _lib.check(plan._lib.usct_plain_forward_fmc_dev(plan.handle, _ptr(md), _ptr(wd), _ptr(data),
-                                                    _ptr(ws), _stream()))
-    return _out(data, m)
+    with plan.lock:   # one call at a time per plan: its workspaces are shared
+        dev = torch.device("cuda", torch.cuda.current_device())
+        md = _to_dev(m, torch.float64, dev)
+        wd = _wavelet(wavelet, nt, dev)
+        data = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev)
+        ws = _workspace(plan.plain_bytes(False), dev)
+        _lib.check(plan._lib.usct_plain_forward_fmc_dev(plan.handle, _ptr(md), _ptr(wd), _ptr(data),
+                                                        _ptr(ws), _stream()))
+        return _out(data, m)
 
 
 def plain_misfit_and_gradient(m, geom, wavelet, dt, h, nt, dobs, src_list=None):
     plan = _setup(m, geom, h, dt, nt, src_list, None, _lib.MODE_FORWARD, 1, None, None)
-    dev = torch.device("cuda", torch.cuda.current_device())
-    md = _to_dev(m, torch.float64, dev)
-    wd = _wavelet(wavelet, nt, dev)
-    od = _to_dev(dobs, torch.float32, dev)
-    if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
-        raise ValueError("dobs shape does not match the acquisition")
-    J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
-    g = torch.empty(plan.shape, dtype=torch.float64, device=dev)
-    ws = _workspace(plan.plain_bytes(True), dev)
-    _lib.check(plan._lib.usct_plain_misfit_and_gradient_dev(
-        plan.handle, _ptr(md), _ptr(wd), _ptr(od), _ptr(J), _ptr(g), _ptr(ws), _stream()))
-    return float(np.sum(J.cpu().numpy())), _out(g, m)
+    with plan.lock:   # one call at a time per plan: its workspaces are shared
+        dev = torch.device("cuda", torch.cuda.current_device())
+        md = _to_dev(m, torch.float64, dev)
+        wd = _wavelet(wavelet, nt, dev)
+        od = _to_dev(dobs, torch.float32, dev)
+        if tuple(od.shape) != (plan.n_tx, plan.nt, plan.n_rx):
+            raise ValueError("dobs shape does not match the acquisition")
+        J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
+        g = torch.empty(plan.shape, dtype=torch.float64, device=dev)
+        ws = _workspace(plan.plain_bytes(True), dev)
+        _lib.check(plan._lib.usct_plain_misfit_and_gradient_dev(
+            plan.handle, _ptr(md), _ptr(wd), _ptr(od), _ptr(J), _ptr(g), _ptr(ws), _stream()))
+        return float(np.sum(J.cpu().numpy())), _out(g, m)

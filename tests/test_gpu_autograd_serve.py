@@ -166,3 +166,37 @@ def test_cancel_mid_flight_then_serve_normally():
         [Request(kind="gradient", m=m, geom=geom, wavelet=wav, dt=dt, h=h, nt=nt,
                  dobs=dobs[[3, 9]], src_list=[3, 9], batch=2)], realtime=False)[0]
     assert after.ok and after.J == alone.J and np.array_equal(after.g, alone.g)
+
+
+def test_concurrent_backend_calls_on_one_plan_are_exact():
+    """Four threads calling the backend with the same problem share one cached
+    plan and its workspaces; the plan lock serialises them, so every result
+    equals the single-threaded one bit for bit (the reference's C++ core is
+    reentrant; so is this backend)."""
+    import threading
+    import openusct_gb300.backend as gb
+    c = load("ring2d_point")
+    args = (c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"])
+    J0, g0 = gb.misfit_and_gradient(*args, src_list=c.src_list)
+    d0 = gb.forward_fmc(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, src_list=c.src_list)
+    out, errs = [], []
+
+    def work():
+        try:
+            for _ in range(3):
+                J, g = gb.misfit_and_gradient(*args, src_list=c.src_list)
+                d = gb.forward_fmc(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt,
+                                   src_list=c.src_list)
+                out.append((J, g, d))
+        except Exception as exc:     # reported below
+            errs.append(exc)
+
+    ts = [threading.Thread(target=work) for _ in range(4)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errs, errs
+    assert len(out) == 12
+    for J, g, d in out:
+        assert J == J0 and np.array_equal(g, g0) and np.array_equal(d, d0)

@@ -187,3 +187,14 @@ def test_backend_validates_what_the_kernels_would_read():
     assert gb.misfit(m, G(), np.zeros(5), 1e-7, 1e-3, 5, np.zeros((0, 5, 3)), src_list=[]) == 0.0
     hv = gb.gn_hessian_vector(m, G(), np.zeros(5), 1e-7, 1e-3, 5, np.ones((6, 6)), src_list=[])
     assert np.array_equal(hv, np.zeros((6, 6)))
+
+
+def test_backend_calls_hold_the_plan_lock():
+    """Concurrent calls that hit one cached plan are serialised on its lock
+    (the plan's workspaces are shared); the cache itself is guarded."""
+    import inspect
+    from openusct_gb300 import backend as gb
+    for fn in (gb.forward_fmc, gb.misfit_and_gradient, gb.misfit, gb.gn_hessian_vector):
+        src = inspect.getsource(fn)
+        assert "with plan.lock:" in src, fn.__name__
+    assert "_PLANS_LOCK" in inspect.getsource(gb.get_plan)
