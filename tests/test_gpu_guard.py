@@ -1,7 +1,7 @@
 """Canary guard bands: every device buffer the library writes is followed by
 1 MiB of a known byte pattern, and the pattern must survive a full gradient
-(and forward, Born and TFM) run -- the check that stands in for a memory
-sanitizer on this pool (SURVEY-style race/overrun detection)."""
+(and forward, Born and TFM) run -- an overrun check that needs no memory
+sanitizer."""
 
 import ctypes
 
