@@ -15,8 +15,8 @@ CASES = ["ring2d_point", "ring2d_sponge", "ring2d_aperture", "cyl3d_point", "cyl
 # FP32-vs-FP64 tolerances per fixture (relative L2).  Traces: 1e-5 on smooth
 # models; the odd* models are per-cell white noise (high-wavenumber fields) and
 # get 1e-4.  Gradients: 1e-4 where the residual is a sizeable part of the data
-# (the benchmark configurations' regime: the reference's own parity problems and most test
-# setups).  cyl3d_point / cyl3d_aperture are nearly converged (|r|/|d| = 0.15%
+# (the benchmark configurations' regime: the reference's own parity problems
+# and most test setups).  cyl3d_point / cyl3d_aperture are nearly converged (|r|/|d| = 0.15%
 # and 0.6%): there the FP32 trace noise (~2e-7 of the data) is 1e-4 of the
 # residual and the FP64 adjoint of that residual alone reproduces the observed
 # 3e-3 / 3e-4 gradient error, so their bound is the conditioning, not the
