@@ -492,27 +492,34 @@ def main():
     del bws, fws
     torch.cuda.empty_cache()
     e2e = None
-    if rank == 0:
-        m0_h = prob.m0
-        dobs_h = dobs.double().cpu().numpy()
-        kw = dict(src_list=shots, batch=C, ckpt_k=ckpt or None)
-        call = (lambda: backend.gn_hessian_vector(m0_h, prob.geom, prob.wavelet, prob.dt, prob.h,
-                                                  prob.nt, prob.v, **kw)) if mode == "gn" else \
-            (lambda: backend.misfit_and_gradient(m0_h, prob.geom, prob.wavelet, prob.dt, prob.h,
-                                                 prob.nt, dobs_h, **kw)[1])
-        call()   # first call builds the plan (and, for small grids, captures graphs)
-        t0 = time.perf_counter()
-        ne = 1 if cells * C > (1 << 24) else 5
-        for _ in range(ne):
-            gh = call()
-        te = (time.perf_counter() - t0) / ne
-        h2d = m0_h.nbytes + prob.wavelet.nbytes + (prob.v.nbytes if mode == "gn" else
-                                                    C * prob.nt * plan.n_rx * 4)
-        e2e = {"value": C / te, "unit": "shots/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(gh.nbytes + (0 if mode == "gn" else 8 * C)),
-               "api": "openusct_gb300.backend." + ("gn_hessian_vector" if mode == "gn"
-                                                   else "misfit_and_gradient")}
-        backend.release()
+    # every rank runs its own batch through the public API (replicas), timed
+    # between barriers; the job's rate uses the slowest rank
+    m0_h = prob.m0
+    dobs_h = dobs.double().cpu().numpy()
+    kw = dict(src_list=shots, batch=C, ckpt_k=ckpt or None)
+    call = (lambda: backend.gn_hessian_vector(m0_h, prob.geom, prob.wavelet, prob.dt, prob.h,
+                                              prob.nt, prob.v, **kw)) if mode == "gn" else \
+        (lambda: backend.misfit_and_gradient(m0_h, prob.geom, prob.wavelet, prob.dt, prob.h,
+                                             prob.nt, dobs_h, **kw)[1])
+    call()   # first call builds the plan (and, for small grids, captures graphs)
+    ne = 1 if cells * C > (1 << 24) else 5
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ne):
+        gh = call()
+    te = (time.perf_counter() - t0) / ne
+    if world > 1:
+        tt = torch.tensor([te], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        te = float(tt.item())
+    h2d = m0_h.nbytes + prob.wavelet.nbytes + (prob.v.nbytes if mode == "gn" else
+                                                C * prob.nt * plan.n_rx * 4)
+    e2e = {"value": C * world / te, "unit": "shots/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(gh.nbytes + (0 if mode == "gn" else 8 * C)),
+           "api": "openusct_gb300.backend." + ("gn_hessian_vector" if mode == "gn"
+                                               else "misfit_and_gradient")}
+    backend.release()
 
     # plain one-shot-per-launch GPU form, same workload, one shot
     plain = None
