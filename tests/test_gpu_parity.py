@@ -372,3 +372,24 @@ def test_cpp_example_against_the_oracle(tmp_path):
                                         p["nt"], d, misfit_type="gcn")
     assert abs(vals["gcn_J"] / Jg - 1) < 1e-4
     assert abs(vals["gcn_grad_sum_abs"] / np.abs(gg).sum() - 1) < 1e-4
+
+
+@pytest.mark.parametrize("mt", ["l2", "gcn"])
+def test_windows_with_footprints_and_sponge_bit_exact(mt):
+    """Data windows combined with finite-aperture elements (and, in 2D, the
+    sponge): the device equals the FP32 restatement bit for bit."""
+    for name in ("ring2d_aperture", "cyl3d_aperture", "ring2d_sponge"):
+        c = load(name)
+        a = c.args()
+        rng = np.random.default_rng(21)
+        W = rng.uniform(0.0, 1.0, (len(a["src_list"]), c.nt, len(c["idx"])))
+        Jr, gr = oracle.misfit_and_gradient32(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt,
+                                              c["dobs"], a["sponge"], a["src_list"],
+                                              a["footprints"], C=2, misfit_type=mt,
+                                              time_weights=W)
+        J, g, Js = gb().misfit_and_gradient(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt,
+                                            c["dobs"], a["sponge"], a["src_list"], misfit_type=mt,
+                                            footprints=a["footprints"], time_weights=W, batch=2,
+                                            ckpt_k=7, return_per_shot=True)
+        assert np.array_equal(g, gr), name
+        assert np.allclose(Js, Jr, rtol=1e-12, atol=0), name
