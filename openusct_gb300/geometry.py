@@ -166,6 +166,122 @@ class CylinderGeometry:
         return self.xyz - self.domain_m / 2.0
 
 
+def fibonacci_directions(n, hemisphere=False):
+    """n near-uniform unit vectors on the sphere (or its upper half) along a
+    golden-angle spiral (geometry.py:140-147): cos(polar) steps uniformly,
+    azimuth advances by pi (1 + sqrt 5) per element."""
+    i = np.arange(n) + 0.5
+    cz = (1.0 - i / n) if hemisphere else (1.0 - 2.0 * i / n)
+    rr = np.sqrt(np.clip(1.0 - cz * cz, 0.0, 1.0))
+    az = np.pi * (1.0 + 5.0 ** 0.5) * i
+    return np.column_stack([rr * np.cos(az), rr * np.sin(az), cz])
+
+
+@dataclass
+class ShellGeometry:
+    """Elements on a spherical shell or its upper half (ShellArray, SphereArray,
+    HemisphereArray semantics, geometry.py:150-196), on a cubic grid."""
+
+    n_elements: int
+    radius_m: float
+    domain_m: float
+    h: float
+    hemisphere: bool = False
+    idx: list = field(init=False)
+    n: int = field(init=False)
+
+    def __post_init__(self):
+        self.n = int(round(self.domain_m / self.h)) + 1
+        c = self.domain_m / 2.0
+        self.xyz = c + self.radius_m * fibonacci_directions(self.n_elements, self.hemisphere)
+        self.idx = [(int(round(z / self.h)), int(round(y / self.h)), int(round(x / self.h)))
+                    for x, y, z in self.xyz]
+
+    @property
+    def grid_shape(self):
+        return (self.n, self.n, self.n)
+
+    def element_index(self, k):
+        return self.idx[k]
+
+    @property
+    def element_positions(self):
+        return self.xyz - self.domain_m / 2.0
+
+    @property
+    def array_type(self):
+        return "hemisphere" if self.hemisphere else "sphere"
+
+
+def tangent_basis(normal):
+    """Unit vector(s) spanning the plane normal to ``normal``: one in 2D (the
+    normal turned by 90 degrees), two in 3D from cross products with the z axis
+    (the x axis when the normal is within ~25 degrees of z) (geometry.py:199-209)."""
+    normal = np.asarray(normal, float)
+    if normal.size == 2:
+        return [np.array([-normal[1], normal[0]])]
+    ax = np.array([0.0, 0.0, 1.0])
+    if abs(np.dot(normal, ax)) > 0.9:
+        ax = np.array([1.0, 0.0, 0.0])
+    u = np.cross(normal, ax)
+    u /= np.linalg.norm(u)
+    return [u, np.cross(normal, u)]
+
+
+def build_footprints(geom, width_m, shape="flat", height_m=None, max_pts=9):
+    """Finite-aperture footprints on the grid (geometry.build_footprints,
+    geometry.py:212-278): each element is a flat aperture in the plane tangent to
+    the array surface -- "rect" (width x height; in 2D a segment), "disc" (an
+    ellipse with those axes), "flat" (a width x width square) or "point" (also
+    any aperture no wider than a cell) -- sampled on an up to ``max_pts``-point
+    grid per axis, snapped to the nearest cells (clipped to the grid), each cell
+    once in first-hit order, equal weights summing to one.  For cylinders the
+    normal is radial in the ring plane, so width runs around the ring and height
+    along its axis.  Returns a list over elements of (idx_list, weights)."""
+    pos = np.asarray(geom.element_positions, float)
+    dim = pos.shape[1]
+    half = geom.domain_m / 2.0
+    h = geom.h
+    n = geom.n
+    if height_m is None or shape == "flat":
+        height_m = width_m
+    as_point = shape == "point" or (width_m <= h and height_m <= h)
+    cylinder = getattr(geom, "array_type", "") == "cylinder"
+
+    def samples(extent):
+        npt = int(np.clip(round(extent / h) + 1, 1, max_pts))
+        return np.linspace(-extent / 2.0, extent / 2.0, npt) if npt > 1 else np.zeros(1)
+
+    out = []
+    for k in range(len(pos)):
+        if as_point:
+            out.append(([geom.element_index(k)], np.array([1.0])))
+            continue
+        p = pos[k]
+        radial = p.copy()
+        if cylinder:
+            radial[2] = 0.0
+        norm = np.linalg.norm(radial)
+        normal = radial / norm if norm > 0 else np.eye(dim)[0]
+        tangents = tangent_basis(normal)
+        extents = [width_m] + ([height_m] if len(tangents) > 1 else [])
+        axes = [samples(e) for e in extents]
+        cells = {}
+        for off in np.array(np.meshgrid(*axes)).reshape(len(axes), -1).T:
+            if shape == "disc":
+                u = off[0] / (width_m / 2.0 + 1e-30)
+                v = (off[1] / (height_m / 2.0 + 1e-30)) if len(off) > 1 else 0.0
+                if u * u + v * v > 1.0 + 1e-9:
+                    continue
+            disp = sum(o * t for o, t in zip(off, tangents))
+            xyz = p + half + disp
+            cell = tuple(int(np.clip(round(xyz[d] / h), 0, n - 1)) for d in range(dim - 1, -1, -1))
+            cells[cell] = True
+        idx_list = list(cells.keys())
+        out.append((idx_list, np.full(len(idx_list), 1.0 / len(idx_list))))
+    return out
+
+
 @dataclass
 class IndexGeometry:
     """Elements given directly as grid-index tuples (GridArray semantics)."""

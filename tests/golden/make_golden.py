@@ -28,6 +28,9 @@ own tests:
                      tapered mute after the direct arrival, L2 and GCN
 * pwindow2d       -- fwi.p_window_weights (fwi.py:663-699) of the ring2d_point
                      data (and of the parity2d data, 16 transmits)
+* footprints      -- geometry.build_footprints (geometry.py:212-278) for rings,
+                     cylinders and spherical shells, every aperture shape, and
+                     the element indices of SphereArray / HemisphereArray
 * tfm2d / tfm3d   -- imaging.tfm (imaging.py:27-74): the reference's point-
                      scatterer dataset of simulation/tests/test_imaging.py:18-38
                      (16-element ring, scattered field only) and a small 3D
@@ -241,6 +244,25 @@ def main():
             out["m_" + key] = m_rec
             out["hist_" + key] = np.asarray(hist)
         save("invert2d", **out)
+
+    # --- element footprints and shell arrays (geometry.py:140-278) -------------
+    if want("footprints"):
+        from ringfwi.geometry import HemisphereArray, SphereArray
+        gs = {"ring": RingArray(n_elements=12, radius_m=0.02, domain_m=0.05, h=1.0e-3),
+              "cyl": CylinderArray(n_rings=3, per_ring=10, radius_m=0.012, height_m=0.012,
+                                   domain_m=0.032, h=8.0e-4),
+              "sphere": SphereArray(20, 0.012, 0.032, 8.0e-4),
+              "hemi": HemisphereArray(16, 0.012, 0.032, 8.0e-4)}
+        cases = [("flat", 0.004, None), ("rect", 0.005, 0.003), ("disc", 0.005, 0.004),
+                 ("point", 0.004, None), ("rect", 0.0005, 0.0005), ("disc", 0.02, 0.02)]
+        out = {}
+        for gname, gobj in gs.items():
+            out[f"{gname}_idx"] = np.asarray(gobj.idx, np.int32)
+            for ci, (shp, w, hgt) in enumerate(cases):
+                fp = build_footprints(gobj, width_m=w, shape=shp, height_m=hgt)
+                p_, c_, w_ = _fp_csr(fp)
+                out[f"{gname}_{ci}_ptr"], out[f"{gname}_{ci}_idx"], out[f"{gname}_{ci}_w"] = p_, c_, w_
+        save("footprints", **out)
 
     # --- TFM imaging (imaging.py:27-74) -----------------------------------------
     def tfm_case(name, geom_t, shape, h_t, dt_t, nt_t, f0, centre_frac, radius_scat, npix,

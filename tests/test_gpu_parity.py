@@ -393,3 +393,31 @@ def test_windows_with_footprints_and_sponge_bit_exact(mt):
                                             ckpt_k=7, return_per_shot=True)
         assert np.array_equal(g, gr), name
         assert np.allclose(Js, Jr, rtol=1e-12, atol=0), name
+
+
+def test_sphere_array_with_disc_apertures_vs_fp64():
+    """A spherical-shell array (SphereArray semantics) with disc apertures
+    built by geometry.build_footprints: traces and gradient against the FP64
+    oracle, and bit for bit against the FP32 restatement."""
+    from openusct_gb300.geometry import ShellGeometry, build_footprints, ricker
+    h = 8.0e-4
+    shell = ShellGeometry(24, 0.012, 0.032, h)
+    fps = build_footprints(shell, width_m=0.003, shape="disc", height_m=0.003)
+    n = shell.n
+    rng = np.random.default_rng(4)
+    c0 = 1500.0 + 40.0 * rng.standard_normal((n, n, n))
+    m_true = 1.0 / (c0 * c0)
+    m0 = np.full((n, n, n), 1.0 / 1500.0 ** 2)
+    dt, nt = 0.3 * h / 1700.0, 160
+    wav = ricker(nt, dt, 0.6e6)
+    sl = [0, 7, 15]
+    d64 = oracle.forward_fmc(m_true, shell.idx, wav, dt, h, nt, None, sl, fps)
+    d32 = gb().forward_fmc(m_true, shell, wav, dt, h, nt, None, sl, fps)
+    assert rel_l2(d32, d64) < 1e-4
+    Jr, gr = oracle.misfit_and_gradient32(m0, shell.idx, wav, dt, h, nt, d64, None, sl, fps, C=4)
+    J, g, Js = gb().misfit_and_gradient(m0, shell, wav, dt, h, nt, d64, None, sl,
+                                        footprints=fps, batch=4, return_per_shot=True)
+    assert np.array_equal(g, gr)
+    J64, g64 = oracle.misfit_and_gradient(m0, shell.idx, wav, dt, h, nt, d64, None, sl, fps, k=20)
+    assert abs(J - J64) <= 1e-4 * J64
+    assert rel_l2(g, g64) < 1e-4

@@ -198,3 +198,38 @@ def test_backend_calls_hold_the_plan_lock():
         src = inspect.getsource(fn)
         assert "with plan.lock:" in src, fn.__name__
     assert "_PLANS_LOCK" in inspect.getsource(gb.get_plan)
+
+
+def _fp_csr(footprints):
+    ptr, cells, w = [0], [], []
+    for idxs, ws in footprints:
+        for c, wi in zip(idxs, ws):
+            cells.append(tuple(int(a) for a in c))
+            w.append(float(wi))
+        ptr.append(len(cells))
+    return np.asarray(ptr, np.int32), np.asarray(cells, np.int32), np.asarray(w)
+
+
+def test_geometry_and_footprints_equal_the_references():
+    """Element placement of rings, cylinders, spheres and hemispheres and the
+    finite-aperture footprints of every shape equal the reference's
+    (footprints fixture) exactly: the same cells in the same order, the same
+    weights."""
+    import os
+    from golden_util import GOLDEN
+    from openusct_gb300.geometry import (CylinderGeometry, RingGeometry, ShellGeometry,
+                                         build_footprints)
+    z = np.load(os.path.join(GOLDEN, "footprints.npz"))
+    gs = {"ring": RingGeometry(12, 0.02, 0.05, 1.0e-3),
+          "cyl": CylinderGeometry(3, 10, 0.012, 0.012, 0.032, 8.0e-4),
+          "sphere": ShellGeometry(20, 0.012, 0.032, 8.0e-4),
+          "hemi": ShellGeometry(16, 0.012, 0.032, 8.0e-4, hemisphere=True)}
+    cases = [("flat", 0.004, None), ("rect", 0.005, 0.003), ("disc", 0.005, 0.004),
+             ("point", 0.004, None), ("rect", 0.0005, 0.0005), ("disc", 0.02, 0.02)]
+    for gname, g in gs.items():
+        assert np.array_equal(np.asarray(g.idx, np.int32), z[f"{gname}_idx"]), gname
+        for ci, (shp, w, hgt) in enumerate(cases):
+            p, c, wt = _fp_csr(build_footprints(g, width_m=w, shape=shp, height_m=hgt))
+            assert np.array_equal(p, z[f"{gname}_{ci}_ptr"]), (gname, ci)
+            assert np.array_equal(c, z[f"{gname}_{ci}_idx"]), (gname, ci)
+            assert np.array_equal(wt, z[f"{gname}_{ci}_w"]), (gname, ci)
