@@ -33,6 +33,12 @@
  * respect to the host unless stated.  Scratch memory is caller-provided
  * ("workspaces"), sized by the *_bytes queries, so callers keep control of
  * HBM (the serving engine admits requests against these sizes).
+ *
+ * Threads: different plans may be used concurrently (from any threads and
+ * streams); calls on one plan, or on one workspace, must not overlap -- a plan
+ * holds its captured graphs and tensor-map cache.  The host-pointer entry
+ * points create a private plan per call and are reentrant, like the
+ * reference's core.
  */
 #ifndef USCT_GB300_H
 #define USCT_GB300_H
