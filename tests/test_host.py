@@ -233,3 +233,20 @@ def test_geometry_and_footprints_equal_the_references():
             assert np.array_equal(p, z[f"{gname}_{ci}_ptr"]), (gname, ci)
             assert np.array_equal(c, z[f"{gname}_{ci}_idx"]), (gname, ci)
             assert np.array_equal(wt, z[f"{gname}_{ci}_w"]), (gname, ci)
+
+
+def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
+    """The autotuner's cache: a stored best launch shape is found again by
+    (dimension, grid, batch width), other keys miss, a corrupt file is
+    ignored."""
+    from openusct_gb300 import autotune
+    path = tmp_path / "tune.json"
+    monkeypatch.setenv("OPENUSCT_GB300_CACHE", str(path))
+    assert autotune.lookup((64, 64, 64), 16) is None
+    autotune._save_cache({autotune.key((64, 64, 64), 16): {"tile": [32, 8, 0, 1], "results": []}})
+    assert autotune.lookup((64, 64, 64), 16) == (32, 8, 0, 1)
+    assert autotune.lookup((64, 64, 64), 32) is None
+    assert autotune.lookup((64, 64), 16) is None
+    path.write_text("{not json")
+    assert autotune.lookup((64, 64, 64), 16) is None
+    assert autotune._parse_tiles("64x4x0x1x6x4,32x8") == [(64, 4, 0, 1, 6, 4), (32, 8, 0)]
