@@ -147,7 +147,7 @@ def test_cancel_mid_flight_then_serve_normally():
     n = geom.n
     m = np.full((n, n), 1.0 / 1500.0 ** 2)
     dt = 0.3 * h / 1500.0
-    nt = 600
+    nt = 1500      # one shot per batch: about a second for all 64 batches
     wav = ricker(nt, dt, 1e6)
     dobs = gb.forward_fmc(m * 0.98, geom, wav, dt, h, nt)
     long_req = Request(kind="gradient", m=m, geom=geom, wavelet=wav, dt=dt, h=h, nt=nt,
@@ -155,7 +155,7 @@ def test_cancel_mid_flight_then_serve_normally():
     short = Request(kind="gradient", m=m, geom=geom, wavelet=wav, dt=dt, h=h, nt=nt,
                     dobs=dobs[[3, 9]], src_list=[3, 9], batch=2, arrival=0.0)
     eng = Engine(GpuExecutor(), budget_bytes=40 << 30, max_active=1)
-    threading.Timer(0.15, long_req.cancel).start()
+    threading.Timer(0.25, long_req.cancel).start()
     res = eng.run_stream([long_req], realtime=False)
     assert not res[0].ok and res[0].error.startswith("Cancelled")
     k = int(res[0].error.split("after ")[1].split(" of")[0])
