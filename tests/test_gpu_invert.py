@@ -223,3 +223,16 @@ def test_pipeline_simulate_then_fwi_plugin():
     reg = _Registry()
     register(reg)
     assert reg.entries["fwi"] == (fwi_from_dataset, "model")
+
+
+def test_readme_quick_start_runs():
+    """The README's quick start, as written there (n_iter shortened)."""
+    from openusct_gb300 import backend as gb, problems
+    from openusct_gb300.invert import invert
+    p = problems.ring2d(seed=0)
+    d = gb.forward_fmc(p.m_true, p.geom, p.wavelet, p.dt, p.h, p.nt)
+    assert d.shape == (64, 1500, 64)
+    J, g = gb.misfit_and_gradient(p.m0, p.geom, p.wavelet, p.dt, p.h, p.nt, d)
+    assert J > 0 and g.shape == p.m0.shape
+    m, hist = invert(p.m0, p.geom, p.wavelet, p.dt, p.h, p.nt, d, n_iter=2)
+    assert hist[-1] < hist[0] and m.shape == p.m0.shape
