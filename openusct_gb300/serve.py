@@ -41,6 +41,8 @@ class Request:
     src_list: list | None = None
     footprints: list | None = None
     sponge: np.ndarray | None = None
+    misfit_type: str = "l2"        # gradient requests: "l2" or "gcn"
+    time_weights: object = None    # gradient requests: one (nt, n_rx) window per transmit
     arrival: float = 0.0           # seconds after the stream starts
     rid: int = -1
     batch: int | None = None
@@ -147,7 +149,8 @@ class GpuExecutor:
 
     def run(self, req, plan):
         torch = self.torch
-        from .backend import _grid_array, _ptr, _stream, _wavelet
+        from .backend import (_check_misfit, _grid_array, _ptr, _stream, _time_weights,
+                              _wavelet)
         lib = plan._lib
         dev = self.device
         st = torch.cuda.Stream(device=dev)
@@ -179,6 +182,8 @@ class GpuExecutor:
                 return {"traces": data.cpu().numpy()}
             if req.dobs is None or np.shape(req.dobs) != (plan.n_tx, plan.nt, plan.n_rx):
                 raise ValueError(f"dobs must have shape {(plan.n_tx, plan.nt, plan.n_rx)}")
+            mt = _check_misfit(req.misfit_type)
+            tw = _time_weights(req.time_weights, plan, dev)
             dobs = torch.from_numpy(np.ascontiguousarray(req.dobs, np.float32)).to(dev)
             bws = torch.empty(plan.batch_bytes(_lib.MODE_GRADIENT), dtype=torch.uint8, device=dev)
             J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
@@ -188,8 +193,8 @@ class GpuExecutor:
             for b in batches():
                 _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
                                                   _lib.MODE_GRADIENT, None, s))
-                _lib.check(lib.usct_batch_misfit(plan.handle, _ptr(bws), b, _ptr(dobs), _ptr(J),
-                                                 s))
+                _lib.check(lib.usct_batch_misfit_tw(plan.handle, _ptr(bws), b, _ptr(dobs), _ptr(tw),
+                                                    mt, _ptr(J), s))
                 _lib.check(lib.usct_batch_backward(plan.handle, _ptr(mws), _ptr(bws), b, s))
             _lib.check(lib.usct_model_gradient(plan.handle, _ptr(mws), _ptr(m), _ptr(g), s))
             plan.check(st)

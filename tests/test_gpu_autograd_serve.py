@@ -200,3 +200,23 @@ def test_concurrent_backend_calls_on_one_plan_are_exact():
     assert len(out) == 12
     for J, g, d in out:
         assert J == J0 and np.array_equal(g, g0) and np.array_equal(d, d0)
+
+
+def test_served_gcn_and_windowed_gradients_match_the_backend():
+    """Gradient requests may carry the GCN misfit and data windows; the served
+    result equals the backend's own call bit for bit (same batch width)."""
+    import openusct_gb300.backend as gb
+    from openusct_gb300.serve import Engine, GpuExecutor, Request
+    c = load("ring2d_window")
+    reqs = [Request(kind="gradient", m=c["m0"], geom=c.geom, wavelet=c.wavelet, dt=c.dt, h=c.h,
+                    nt=c.nt, dobs=c["dobs"], src_list=c.src_list, batch=2, misfit_type=mt,
+                    time_weights=tw)
+            for mt, tw in (("gcn", None), ("l2", c["tw"]), ("gcn", c["tw"]))]
+    res = Engine(GpuExecutor(), budget_bytes=8 << 30, max_active=2).run_stream(reqs,
+                                                                              realtime=False)
+    for r, q in zip(res, reqs):
+        assert r.ok, r.error
+        J, g = gb.misfit_and_gradient(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt, q.dobs,
+                                      src_list=q.src_list, misfit_type=q.misfit_type,
+                                      time_weights=q.time_weights, batch=2)
+        assert np.array_equal(r.g, g) and r.J == J
