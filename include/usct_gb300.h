@@ -325,7 +325,9 @@ int usct_vec_dot_dev(const double* x, const double* y, size_t n, double* ws, voi
  * g (device FP32, nt values: the imaginary part of the inverse DFT of scipy's
  * spectral multiplier, computed by the caller).  data: device FP64
  * [n_tx][nt][n_rx] (the Dataset layout); analytic: device FP32 interleaved
- * (re, im) [n_tx][n_rx][nt], trace-major.
+ * (re, im) [n_tx][n_rx][nt], trace-major.  For even nt the taps at even
+ * offsets must be zero (they are, for scipy's multiplier) and are skipped.
+ * n_tx <= 65535, nt <= 2097120.
  */
 int usct_analytic_dev(const double* data, float* analytic, int n_tx, int nt, int n_rx,
                       const float* taps, void* stream);

@@ -5,21 +5,23 @@
 // with A the analytic signal of each trace (scipy.signal.hilbert along time)
 // and samples outside [0, nt) skipped; the envelope image is |I|.
 //
-// Two kernels:
+// Kernels, in launch order k_real, k_analytic, k_tfm (and k_pwindow):
 //  * k_analytic -- A = x + i (x (*) g): the FFT-based analytic signal written
 //    as a circular convolution of each trace with the imaginary part g of the
 //    inverse DFT of scipy's spectral multiplier (computed on the host, FP64,
-//    handed over as FP32 taps).  FP32 multiply-adds, one block per 16 traces x
-//    256 samples, traces and taps staged in shared memory.  It also transposes
-//    the data from the Dataset layout [tx][n][rx] (FP64) to trace-major
-//    [tx][rx][n] (float2 re/im), so the gathers of neighbouring pixels hit
-//    neighbouring samples of one trace.
-//  * k_tfm -- one thread per pixel: distances in FP64 with the reference's
-//    operation order, kept as FP32 per receiver in shared memory; the sample
+//    handed over as FP32 taps).  FP32 multiply-adds, one lane per trace and
+//    a register ring of taps, traces and taps staged in shared memory.  The
+//    result is trace-major [tx][rx][n] (float2 re/im), so the gathers of
+//    neighbouring pixels hit neighbouring samples of one trace.
+//  * k_real -- the transpose to trace-major (real parts), each FP64 sample
+//    converted once; k_analytic then fills in the imaginary parts.
+//  * k_tfm -- eight threads per pixel, each summing a share of the
+//    transmits: FP32 distances (receivers' kept in shared memory); the sample
 //    index equals NumPy's np.round((d_tx + d_rx) / c * fs) (an FP32 product
-//    decides it except near a half-integer, where the FP64 expression is
-//    formed); the complex samples of one transmit are summed in FP32 over
-//    the receivers (in the reference's order), the transmits in FP64.
+//    decides it except near a half-integer, where the FP64 distances and
+//    expression are formed in the reference's order); the complex samples of
+//    one transmit are summed in FP32 over the receivers (in the reference's
+//    order), the transmits in FP64.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -30,9 +32,13 @@ int usct_internal_error(int code, const char* msg);   // usct_engine.cu
 
 namespace {
 
-constexpr int kHT = 16;     // traces per block
-constexpr int kHN = 256;    // output samples per block
-constexpr int kHM = 64;     // input samples per stage
+constexpr int kAW = 8;              // warps per block
+constexpr int kAB = 16;             // outputs per thread (a power of two)
+constexpr int kAM = 64;             // input samples per stage
+constexpr int kAN = kAW * kAB;      // outputs per block
+constexpr int kAT = 64;             // traces per block: two per lane
+constexpr int kAG = kAN + kAM - 1;  // taps per stage
+constexpr int kAQ = kAT * kAM / (kAW * 32);   // staged samples per thread
 
 int cuda_status(cudaError_t e) {
     if (e == cudaSuccess) return USCT_OK;
@@ -40,76 +46,151 @@ int cuda_status(cudaError_t e) {
                                cudaGetErrorString(e));
 }
 
-// block (64, 4): thread (tx, ty) accumulates traces 4*ty..4*ty+3 of the block
-// at output samples n0 + tx + 64*b, b = 0..3 (a variant with 8 traces per
-// thread and paired multiply-adds measured 11 % slower).  For even nt the taps
-// are zero at even offsets (the host passes exact zeros there) and are skipped.
-__global__ void __launch_bounds__(256) k_analytic(const double* __restrict__ data,
-                                                  float2* __restrict__ out, int n_tx, int nt,
-                                                  int n_rx, const float* __restrict__ g) {
-    __shared__ float xs[kHT][kHM + 1];
-    __shared__ float gs[kHN + kHM];
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = tx + 64 * ty;
-    const long long ntr = (long long)n_tx * n_rx;
-    const long long t0 = (long long)blockIdx.y * kHT;
-    const int n0 = blockIdx.x * kHN;
-    float acc[4][4];
+// Block (32 * kAW): lane l owns traces tb + l and tb + l + 32, warp w owns the
+// outputs nb + S*b, b < kAB, where S = 2 for even nt (the taps vanish at even
+// offsets, so an output only meets inputs of the other parity, and the warp
+// pair (2v, 2v+1) covers 2*kAB consecutive outputs) and S = 1 for odd nt.
+// Output b at input step k needs the tap G[b - k] (G[q] = g[nb - m_first +
+// S*q]), so a thread keeps the kAB taps of the current step in a register
+// ring and loads one new tap per step: per step two shared loads of the
+// traces' samples, one broadcast load of a tap and 2*kAB multiply-adds.  The
+// stages are double-buffered: the next stage's samples and taps are loaded
+// into registers before this stage's multiply-adds and stored after them, one
+// barrier per stage.  Every output sums its inputs in increasing m, one fmaf
+// each.  The samples come from the real parts k_real wrote (out[2*(t*nt + m)]);
+// only the imaginary parts are written here.
+template <int S>
+__global__ void __launch_bounds__(kAW * 32, 2) k_analytic(float* __restrict__ out, long long ntr,
+                                                          int nt, const float* __restrict__ g) {
+    __shared__ float xs[2][kAT][kAM + 1];   // odd pitch: the lanes' rows fall in distinct banks
+    __shared__ float gs[2][kAG];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int n0 = blockIdx.y * kAN;
+    const int nb = (S == 1) ? n0 + kAB * w : n0 + 2 * kAB * (w >> 1) + (w & 1);
+    const int par = (S == 1) ? 0 : 1 - (w & 1);   // parity of the inputs this warp meets
+    const long long tb = (long long)blockIdx.x * kAT;
+    // staging: thread x stages sample (x & 63) of traces (x >> 6) + 4q, q < kAQ;
+    // a warp reads 32 consecutive samples of one trace
+    const int smm = threadIdx.x & (kAM - 1), stt = threadIdx.x / kAM;
+    float pf[kAQ];
+    float pg = 0.f;
+    auto load = [&](int m0) {
+        const int m = m0 + smm;
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
-    for (int m0 = 0; m0 < nt; m0 += kHM) {
-        // traces t0..t0+15, samples m0..m0+63 (trace t = i*n_rx + j reads data[i][m][j])
-        for (int e = tid; e < kHT * kHM; e += 256) {
-            const int tt = e / kHM, mm = e % kHM;
-            const long long t = t0 + tt;
-            const int m = m0 + mm;
-            float v = 0.f;
-            if (t < ntr && m < nt) {
-                const long long i = t / n_rx, j = t % n_rx;
-                v = (float)data[(i * nt + m) * n_rx + j];
-            }
-            xs[tt][mm] = v;
+        for (int q = 0; q < kAQ; ++q) {
+            const long long t = tb + stt + (kAW * 32 / kAM) * q;
+            pf[q] = (t < ntr && m < nt) ? out[2 * (t * nt + m)] : 0.f;
         }
-        // taps g[(n - m) mod nt] for n - m in [n0 - m0 - 63, n0 - m0 + 255]
-        for (int e = tid; e < kHN + kHM; e += 256) {
-            long long d = (long long)n0 - m0 - (kHM - 1) + e;
+        if (threadIdx.x < kAG) {
+            int d = n0 - m0 - (kAM - 1) + (int)threadIdx.x;   // |d| < nt + kAN: int suffices
             d %= nt;
             if (d < 0) d += nt;
-            gs[e] = g[d];
+            pg = g[d];
         }
-        __syncthreads();
-        const int mlim = min(kHM, nt - m0);
-        // for even nt the taps vanish at even offsets: a thread's outputs all
-        // have the parity of tx (n0, m0 and 64*b are even), so only inputs of
-        // the other parity contribute
-        const int mstart = (nt & 1) ? 0 : ((tx + 1) & 1);
-        const int mstep = (nt & 1) ? 1 : 2;
-        for (int mm = mstart; mm < mlim; mm += mstep) {
-            float xv[4];
+    };
+    auto store = [&](int buf) {
 #pragma unroll
-            for (int a = 0; a < 4; ++a) xv[a] = xs[4 * ty + a][mm];
+        for (int q = 0; q < kAQ; ++q) xs[buf][stt + (kAW * 32 / kAM) * q][smm] = pf[q];
+        if (threadIdx.x < kAG) gs[buf][threadIdx.x] = pg;
+    };
+    float acc0[kAB], acc1[kAB];
 #pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const float gv = gs[tx + 64 * b - mm + (kHM - 1)];
+    for (int b = 0; b < kAB; ++b) acc0[b] = acc1[b] = 0.f;
+    load(0);
+    store(0);
+    __syncthreads();
+    int buf = 0;
+    for (int m0 = 0; m0 < nt; m0 += kAM) {
+        const bool more = m0 + kAM < nt;
+        if (more) load(m0 + kAM);
+        // step k of this stage is input m0 + par + S*k; G[q] = gp[S*q] with
+        // q in [-(kAM/S - 1), kAB - 1], inside gs for every warp
+        const float* x0 = &xs[buf][lane][par];
+        const float* x1 = &xs[buf][lane + 32][par];
+        const float* gp = &gs[buf][nb - n0 - par + kAM - 1];
+        float wr[kAB];   // wr[q & (kAB-1)] = G[q] for the kAB live q
 #pragma unroll
-                for (int a = 0; a < 4; ++a) acc[a][b] = __fmaf_rn(xv[a], gv, acc[a][b]);
+        for (int b = 1; b < kAB; ++b) wr[b] = gp[S * b];
+        for (int k0 = 0; k0 < kAM / S; k0 += kAB) {
+#pragma unroll
+            for (int k = 0; k < kAB; ++k) {
+                const int kk = k0 + k;
+                wr[(kAB - k) & (kAB - 1)] = gp[-S * kk];   // G[-kk] replaces G[kAB - kk]
+                const float xv0 = x0[S * kk], xv1 = x1[S * kk];
+#pragma unroll
+                for (int b = 0; b < kAB; ++b) {
+                    const float gv = wr[(b - k) & (kAB - 1)];
+                    acc0[b] = __fmaf_rn(xv0, gv, acc0[b]);
+                    acc1[b] = __fmaf_rn(xv1, gv, acc1[b]);
+                }
             }
         }
+        if (more) store(buf ^ 1);   // the other buffer: every warp left it at the last barrier
         __syncthreads();
+        buf ^= 1;
     }
+    // the imaginary parts only: other blocks still read the real parts
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        const long long t = t0 + 4 * ty + a;
+    for (int h = 0; h < 2; ++h) {
+        const long long t = tb + lane + 32 * h;
         if (t >= ntr) continue;
-        const long long i = t / n_rx, j = t % n_rx;
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const int n = n0 + tx + 64 * b;
-            if (n < nt)
-                out[t * nt + n] = make_float2((float)data[(i * nt + n) * n_rx + j], acc[a][b]);
+        for (int b = 0; b < kAB; ++b) {
+            const int n = nb + S * b;
+            if (n < nt) out[2 * (t * nt + n) + 1] = h ? acc1[b] : acc0[b];
         }
+    }
+}
+
+// Exact FP64 <-> FP32 conversions (IEEE round to nearest even) in integer
+// arithmetic: the hardware conversions issue to the FP64 pipe, of which this
+// part has very little.  Zeros and the normal range take the integer path;
+// subnormal, out-of-range, infinite and NaN values the hardware one.
+__device__ __forceinline__ float f64_to_f32(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e >= 897 && e <= 1150) {   // FP32 exponent e - 896 in [1, 254]
+        const unsigned long long m = b & 0xfffffffffffffULL;
+        unsigned r = ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29);
+        const unsigned rem = (unsigned)(m & 0x1fffffffULL);   // the 29 dropped bits
+        r += (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;
+        return __uint_as_float(r | sign);   // a carry into the exponent is exact (to inf at the top)
+    }
+    if ((b << 1) == 0) return __uint_as_float(sign);
+    return __double2float_rn(x);
+}
+
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e - 1u < 254u) {
+        const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                     ((unsigned long long)(e + 896u) << 52) |
+                                     ((unsigned long long)(u & 0x7fffffu) << 29);
+        return __longlong_as_double((long long)b);
+    }
+    if ((u << 1) == 0) return __longlong_as_double((long long)((unsigned long long)u << 32));
+    return (double)f;
+}
+
+// out[i][j][m] = (data[i][m][j], 0): the Dataset layout to trace-major, each
+// FP64 sample converted to FP32 once.  32 x 32 tiles (m, j) through shared
+// memory, so both the reads (along j) and the writes (along m) are coalesced.
+__global__ void __launch_bounds__(256) k_real(const double* __restrict__ data,
+                                              float2* __restrict__ out, int nt, int n_rx) {
+    __shared__ float tile[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const long long i = blockIdx.z;
+    const int m0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+    for (int r = ty; r < 32; r += 8) {
+        const int m = m0 + r, j = j0 + tx;
+        if (m < nt && j < n_rx) tile[r][tx] = f64_to_f32(data[(i * nt + m) * n_rx + j]);
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        const int j = j0 + r, m = m0 + tx;
+        if (j < n_rx && m < nt) out[(i * n_rx + j) * nt + m] = make_float2(tile[tx][r], 0.f);
     }
 }
 
@@ -125,15 +206,86 @@ __device__ __forceinline__ double dist(const double (&r)[3], const double* __res
     return sqrt(s);
 }
 
-// One thread per pixel, 128 pixels per block.  Each thread first writes its
-// pixel's receiver distances (FP32) to its own column of shared memory, then
-// for every transmit adds the samples of all receivers (FP32 within a
-// transmit, FP64 across transmits).  The index is decided
-// in FP32, (d_tx + d_rx) * (fs / c), whose error against the reference's FP64
-// round((d_tx + d_rx) / c * fs) is below 1e-6 * v + 1e-5 samples; only when the
-// FP32 value lies within that margin of a half-integer is the FP64 expression
-// formed, in the reference's order -- so every index equals NumPy's.
-constexpr int kTB = 128;
+// ---- float-float (FP32 pair) arithmetic: value = x + y, |y| <= ulp(x)/2 ----
+// (exact error-free transformations: Knuth's two-sum, Dekker's fast two-sum,
+// the fused multiply-add product error; the build contracts nothing)
+__device__ __forceinline__ float2 ff_two_sum(float a, float b) {
+    const float s = a + b, bb = s - a;
+    return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ float2 ff_fast_two_sum(float a, float b) {   // |a| >= |b| or a == 0
+    const float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+__device__ __forceinline__ float2 ff_from(double x) {
+    const float h = f64_to_f32(x);
+    return make_float2(h, f64_to_f32(x - f32_to_f64(h)));
+}
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+    const float2 s = ff_two_sum(a.x, b.x);
+    return ff_fast_two_sum(s.x, s.y + (a.y + b.y));
+}
+__device__ __forceinline__ float2 ff_sq(float2 a) {
+    const float p = a.x * a.x;
+    float e = __fmaf_rn(a.x, a.x, -p);
+    e = __fmaf_rn(2.f * a.x, a.y, e);
+    return ff_fast_two_sum(p, e);
+}
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    return ff_fast_two_sum(p, e);
+}
+__device__ __forceinline__ float2 ff_sqrt(float2 a) {   // one Newton step from sqrtf
+    if (!(a.x > 0.f)) return make_float2(0.f, 0.f);
+    const float s = sqrtf(a.x);
+    const float r = __fmaf_rn(-s, s, a.x) + a.y;
+    return ff_fast_two_sum(s, r / (2.f * s));
+}
+// |r - p| from float-float coordinates
+template <int DIM>
+__device__ __forceinline__ float2 ff_dist(const float2 (&r)[3], const float2* __restrict__ p) {
+    float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+        const float2 q = ff_sq(ff_add(r[a], make_float2(-p[a].x, -p[a].y)));
+        s = (a == 0) ? q : ff_add(s, q);
+    }
+    return ff_sqrt(s);
+}
+
+// Block (kTP * kTG): kTP pixels, kTG threads per pixel.  The threads of a
+// pixel first write its receiver distances to the pixel's column of shared
+// memory, then thread g of the pixel forms the sums of transmits g, g + kTG,
+// ... (FP32 over the receivers, in receiver order) and parks them in shared
+// memory, where the pixel's first thread adds them to the FP64 sums in
+// transmit order -- the same sums, in the same order, as one thread per
+// pixel, with kTG times the threads in flight.
+//
+// The sample index: v = (d_tx + d_rx) * (fs / c) is formed first in FP32 from
+// the leading halves of the distances below (within 2.4e-7 * v of the FP64
+// value: four roundings of 6e-8), which decides it unless v lies within
+// 1e-6 * v + 1e-5 of a half-integer (about 0.2 % of pairs).  There it is
+// formed in float-float from float-float coordinates (the element
+// coordinates of the current receiver chunk and transmit window staged in
+// shared memory).  That error
+// against the reference's FP64 (d_tx + d_rx) / c * fs is below
+// 1e-11 * v + 4e-13 * (fs / c) * |r|_1 (the second term: the coordinates'
+// float-float rounding, 4 u^2 per coordinate, through |p| <= |r| + |r - p|;
+// over 5e6 random pairs and geometries, arrays offset up to 1000 times their
+// size included, the error stayed below 1.5 % of that bound), and frac(v) - 1/2
+// is then formed with 6e-8 error.  Only where that lies within
+// 1e-11 * v + 2e-7 + 4e-13 * (fs / c) * |r|_1 of zero (about 2 pairs in a
+// million) are the FP64 distances and expression formed, in the reference's
+// order -- so every index equals NumPy's np.round, and FP64 work (slow on
+// this part, and paid by the whole warp when one lane needs it) stays rare.
+constexpr int kTP = 16;    // pixels per block
+constexpr int kTG = 8;     // threads per pixel
+constexpr int kTW = 64;    // transmits per window of parked sums
+constexpr int kTB = kTP * kTG;
+constexpr int kRxChunk = 256;   // receivers whose distances are held at once
 template <int DIM>
 __global__ void __launch_bounds__(kTB) k_tfm(const float2* __restrict__ A, int n_tx, int n_rx,
                                              int nt, const double* __restrict__ tx_pos,
@@ -142,67 +294,113 @@ __global__ void __launch_bounds__(kTB) k_tfm(const float2* __restrict__ A, int n
                                              long long npts, int rx_chunk, double c, double fs,
                                              double* __restrict__ out_re,
                                              double* __restrict__ out_im) {
-    extern __shared__ float drx[];   // [rx_chunk][kTB]
-    const long long p = blockIdx.x * (long long)kTB + threadIdx.x;
-    if (p >= npts) return;
+    extern __shared__ float2 drx[];              // [rx_chunk][kTP] float-float distances
+    __shared__ float2 rxc[kRxChunk * DIM];       // the chunk's receiver coordinates
+    __shared__ float2 txc[kTW * DIM];            // the window's transmit coordinates
+    __shared__ float2 part[kTW][kTP];            // parked per-transmit sums
+    const int px = threadIdx.x % kTP, grp = threadIdx.x / kTP;
+    const long long p = blockIdx.x * (long long)kTP + px;
+    const bool live = p < npts;
     // pixel p of the C-order (ij) grid: the last axis varies fastest
     double r[3] = {0.0, 0.0, 0.0};
-    long long q = p;
+    if (live) {
+        long long q = p;
 #pragma unroll
-    for (int a = DIM - 1; a >= 0; --a) {
-        r[a] = axes[a * npix + (int)(q % npix)];
-        q /= npix;
+        for (int a = DIM - 1; a >= 0; --a) {
+            r[a] = axes[a * npix + (int)(q % npix)];
+            q /= npix;
+        }
     }
-    const float rate = (float)(fs / c);
+    float2 rf[3];
+    float r1 = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        rf[a] = ff_from(r[a]);
+        r1 += fabsf(rf[a].x);
+    }
+    const float2 rate = ff_from(fs / c);
+    const float mabs = 2e-7f + 4e-13f * rate.x * (1.01f * r1);
     const float ntf = (float)nt;
-    float* col = drx + threadIdx.x;
+    const float2* col = drx + px;
     double sre = 0.0, sim = 0.0;
     for (int j0 = 0; j0 < n_rx; j0 += rx_chunk) {
         const int nj = min(rx_chunk, n_rx - j0);
-        for (int jj = 0; jj < nj; ++jj) col[jj * kTB] = (float)dist<DIM>(r, rx_pos, j0 + jj);
-        for (int i = 0; i < n_tx; ++i) {
-            const double dtx = dist<DIM>(r, tx_pos, i);
-            const float dtx32 = (float)dtx;
-            const float2* slab = A + ((long long)i * n_rx + j0) * nt;
-            float pre = 0.f, pim = 0.f;   // this transmit's sum over the receivers
-            // eight receivers at a time: all eight indices first, then eight
-            // independent gathers in flight, then the sums in receiver order
-            // (a skipped sample adds 0, which leaves the sum unchanged)
-            for (int jb = 0; jb < nj; jb += 8) {
-                int kk[8];
+        __syncthreads();   // the previous chunk's coordinates and distances are no longer read
+        for (int e = threadIdx.x; e < nj * DIM; e += kTB)
+            rxc[e] = ff_from(rx_pos[(long long)j0 * DIM + e]);
+        __syncthreads();
+        for (int jj = grp; jj < nj; jj += kTG)
+            drx[jj * kTP + px] = ff_dist<DIM>(rf, rxc + jj * DIM);
+        for (int i0 = 0; i0 < n_tx; i0 += kTW) {
+            const int ni = min(kTW, n_tx - i0);
+            for (int e = threadIdx.x; e < ni * DIM; e += kTB)
+                txc[e] = ff_from(tx_pos[(long long)i0 * DIM + e]);
+            __syncthreads();   // distances and transmit coordinates written
+            for (int ii = grp; ii < ni; ii += kTG) {
+                const int i = i0 + ii;
+                float pre = 0.f, pim = 0.f;   // this transmit's sum over the receivers
+                if (live) {
+                    const float2 dtx = ff_dist<DIM>(rf, txc + ii * DIM);
+                    const float2* slab = A + ((long long)i * n_rx + j0) * nt;
+                    // eight receivers at a time: all eight indices first, then
+                    // eight independent gathers in flight, then the sums in
+                    // receiver order (a skipped sample adds 0, which leaves
+                    // the sum unchanged)
+                    for (int jb = 0; jb < nj; jb += 8) {
+                        int kk[8];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int jj = jb + u;
-                    kk[u] = -1;
-                    if (jj < nj) {
-                        const float v = (dtx32 + col[jj * kTB]) * rate;
-                        const float fr = v - floorf(v);
-                        float kf;
-                        if (fabsf(fr - 0.5f) <= 1e-6f * v + 1e-5f) {
-                            const double s = dtx + dist<DIM>(r, rx_pos, j0 + jj);
-                            kf = (float)rint((s / c) * fs);
-                        } else {
-                            kf = rintf(v);
+                        for (int u = 0; u < 8; ++u) {
+                            const int jj = jb + u;
+                            kk[u] = -1;
+                            if (jj < nj) {
+                                const float2 drj = col[jj * kTP];
+                                // FP32 first: within 2.4e-7 * v of the FP64 value
+                                const float v32 = (dtx.x + drj.x) * rate.x;
+                                float kf = rintf(v32);
+                                if (fabsf((v32 - floorf(v32)) - 0.5f) <= 1e-6f * v32 + 1e-5f) {
+                                    const float2 v = ff_mul(ff_add(dtx, drj), rate);
+                                    const float fl = floorf(v.x);
+                                    const float g = ((v.x - fl) - 0.5f) + v.y;
+                                    if (fabsf(g) <= 1e-11f * v.x + mabs) {
+                                        const double s = dist<DIM>(r, tx_pos, i) +
+                                                         dist<DIM>(r, rx_pos, j0 + jj);
+                                        kf = (float)rint((s / c) * fs);
+                                    } else {
+                                        kf = g > 0.f ? fl + 1.f : fl;
+                                    }
+                                }
+                                if (kf >= 0.f && kf < ntf) kk[u] = (int)kf;
+                            }
                         }
-                        if (kf >= 0.f && kf < ntf) kk[u] = (int)kf;
+                        float2 a[8];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u)
+                            a[u] = kk[u] >= 0 ? slab[(long long)(jb + u) * nt + kk[u]]
+                                              : make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            pre += a[u].x;
+                            pim += a[u].y;
+                        }
                     }
                 }
-                float2 a[8];
-#pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    a[u] = kk[u] >= 0 ? slab[(long long)(jb + u) * nt + kk[u]] : make_float2(0.f, 0.f);
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    pre += a[u].x;
-                    pim += a[u].y;
+                part[ii][px] = make_float2(pre, pim);
+            }
+            __syncthreads();
+            if (grp == 0 && live) {
+                for (int ii = 0; ii < ni; ++ii) {
+                    const float2 v = part[ii][px];
+                    sre += f32_to_f64(v.x);
+                    sim += f32_to_f64(v.y);
                 }
             }
-            sre += (double)pre;
-            sim += (double)pim;
+            __syncthreads();   // parked sums and transmit coordinates consumed
         }
     }
-    out_re[p] = sre;
-    out_im[p] = sim;
+    if (grp == 0 && live) {
+        out_re[p] = sre;
+        out_im[p] = sim;
+    }
 }
 
 // P-arrival mute windows (fwi.py:663-699): one warp per trace of the
@@ -260,11 +458,19 @@ extern "C" int usct_analytic_dev(const double* data, float* analytic, int n_tx, 
     if (!data || !analytic || !taps) return usct_internal_error(USCT_ERR_ARG, "null argument");
     if (n_tx < 1 || nt < 1 || n_rx < 1) return usct_internal_error(USCT_ERR_ARG, "empty data");
     const long long ntr = (long long)n_tx * n_rx;
-    if ((ntr + kHT - 1) / kHT > 65535)
-        return usct_internal_error(USCT_ERR_ARG, "too many traces (n_tx * n_rx > 1048560)");
-    const dim3 grid((nt + kHN - 1) / kHN, (unsigned)((ntr + kHT - 1) / kHT));
-    k_analytic<<<grid, dim3(64, 4), 0, (cudaStream_t)stream>>>(
-        data, reinterpret_cast<float2*>(analytic), n_tx, nt, n_rx, taps);
+    if (n_tx > 65535) return usct_internal_error(USCT_ERR_ARG, "n_tx > 65535");
+    if ((nt + 31) / 32 > 65535)
+        return usct_internal_error(USCT_ERR_ARG, "nt too large (> 2097120 samples)");
+    if ((ntr + kAT - 1) / kAT > 0x7fffffffLL)
+        return usct_internal_error(USCT_ERR_ARG, "too many traces");
+    cudaStream_t s = (cudaStream_t)stream;
+    k_real<<<dim3((n_rx + 31) / 32, (nt + 31) / 32, n_tx), 256, 0, s>>>(
+        data, reinterpret_cast<float2*>(analytic), nt, n_rx);
+    const dim3 grid((unsigned)((ntr + kAT - 1) / kAT), (nt + kAN - 1) / kAN);
+    if (nt % 2 == 0)
+        k_analytic<2><<<grid, kAW * 32, 0, s>>>(analytic, ntr, nt, taps);
+    else
+        k_analytic<1><<<grid, kAW * 32, 0, s>>>(analytic, ntr, nt, taps);
     return cuda_status(cudaGetLastError());
 }
 
@@ -279,22 +485,19 @@ extern "C" int usct_tfm_dev(const float* analytic, int n_tx, int n_rx, int nt, c
     if (!(c > 0.0) || !(fs > 0.0)) return usct_internal_error(USCT_ERR_ARG, "c and fs must be > 0");
     long long npts = 1;
     for (int a = 0; a < dim; ++a) npts *= npix;
-    // every receiver in one pass (the reference's summation order) up to 320
-    // receivers; beyond that in chunks of 320
-    const int rx_chunk = n_rx < 320 ? n_rx : 320;
-    const size_t smem = (size_t)rx_chunk * kTB * sizeof(float);
-    const long long blocks = (npts + kTB - 1) / kTB;
+    // every receiver in one pass (the reference's summation order) up to
+    // kRxChunk receivers; beyond that in chunks of kRxChunk
+    const int rx_chunk = n_rx < kRxChunk ? n_rx : kRxChunk;
+    const size_t smem = (size_t)rx_chunk * kTP * sizeof(float2);
+    const long long blocks = (npts + kTP - 1) / kTP;
     if (blocks > 0x7fffffffLL) return usct_internal_error(USCT_ERR_ARG, "image too large");
     const float2* A = reinterpret_cast<const float2*>(analytic);
     cudaStream_t s = (cudaStream_t)stream;
-    if (dim == 2) {
-        cudaFuncSetAttribute(k_tfm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 320 * kTB * 4);
+    if (dim == 2)
         k_tfm<2><<<(unsigned)blocks, kTB, smem, s>>>(A, n_tx, n_rx, nt, tx_pos, rx_pos, axes, npix,
                                                      npts, rx_chunk, c, fs, out_re, out_im);
-    } else {
-        cudaFuncSetAttribute(k_tfm<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 320 * kTB * 4);
+    else
         k_tfm<3><<<(unsigned)blocks, kTB, smem, s>>>(A, n_tx, n_rx, nt, tx_pos, rx_pos, axes, npix,
                                                      npts, rx_chunk, c, fs, out_re, out_im);
-    }
     return cuda_status(cudaGetLastError());
 }
