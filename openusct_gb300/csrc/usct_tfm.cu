@@ -50,30 +50,47 @@ int cuda_status(cudaError_t e) {
 // outputs nb + S*b, b < kAB, where S = 2 for even nt (the taps vanish at even
 // offsets, so an output only meets inputs of the other parity, and the warp
 // pair (2v, 2v+1) covers 2*kAB consecutive outputs) and S = 1 for odd nt.
-// Output b at input step k needs the tap G[b - k] (G[q] = g[nb - m_first +
-// S*q]), so a thread keeps the kAB taps of the current step in a register
-// ring and loads one new tap per step: per step two shared loads of the
-// traces' samples, one broadcast load of a tap and 2*kAB multiply-adds.  The
-// stages are double-buffered: the next stage's samples and taps are loaded
-// into registers before this stage's multiply-adds and stored after them, one
+// Output b at input step k needs the tap G[b - k]; G[q] = T[cw + q], T the
+// stage's taps g[(n0 - m0 - (kAM-1) + S*i) mod nt].  The outputs are taken in
+// pairs (2j, 2j+1), so step k multiplies each trace's sample by the tap pairs
+// (T[cw - k + 2j], T[cw - k + 2j + 1]), j < kAB/2, in paired multiply-adds
+// (fma.rn.f32x2, two IEEE fmaf per lane).  Those pairs start at indices of one
+// parity on even steps and of the other on odd steps, so shared memory holds
+// the taps pre-paired in both alignments (tp[a][e] = (T[2e+a], T[2e+a+1])) and
+// a thread keeps a register ring of kAB/2 pairs for each: every step loads one
+// new pair, two samples and issues kAB paired multiply-adds.  The stages are
+// double-buffered: the next stage's samples and taps are loaded into
+// registers before this stage's multiply-adds and stored after them, one
 // barrier per stage.  Every output sums its inputs in increasing m, one fmaf
-// each.  The samples come from the real parts k_real wrote (out[2*(t*nt + m)]);
-// only the imaginary parts are written here.
+// each.  The samples come from the real parts k_real wrote
+// (out[2*(t*nt + m)]); only the imaginary parts are written here.
 template <int S>
 __global__ void __launch_bounds__(kAW * 32, 2) k_analytic(float* __restrict__ out, long long ntr,
                                                           int nt, const float* __restrict__ g) {
+    constexpr int kL = (S == 1) ? kAG : (kAG + 1) / 2;   // taps T of one stage
+    constexpr int kP = kL / 2 + 1;                      // pairs per alignment
+    constexpr int kH = kAB / 2;                         // output pairs per thread
     __shared__ float xs[2][kAT][kAM + 1];   // odd pitch: the lanes' rows fall in distinct banks
-    __shared__ float gs[2][kAG];
+    __shared__ float2 tp[2][2][kP];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int n0 = blockIdx.y * kAN;
     const int nb = (S == 1) ? n0 + kAB * w : n0 + 2 * kAB * (w >> 1) + (w & 1);
     const int par = (S == 1) ? 0 : 1 - (w & 1);   // parity of the inputs this warp meets
+    const int cw = (nb - n0 - par + kAM - 1) / S;  // T index of G[0] (exact: even for S = 2)
     const long long tb = (long long)blockIdx.x * kAT;
-    // staging: thread x stages sample (x & 63) of traces (x >> 6) + 4q, q < kAQ;
-    // a warp reads 32 consecutive samples of one trace
+    // staging: thread x stages sample (x & 63) of traces (x >> 6) + 4q, q < kAQ
+    // (a warp reads 32 consecutive samples of one trace), and threads below
+    // 2*kP the tap pair tp[x / kP][x % kP]
     const int smm = threadIdx.x & (kAM - 1), stt = threadIdx.x / kAM;
+    const int pa = threadIdx.x / kP, pe = threadIdx.x % kP;
     float pf[kAQ];
-    float pg = 0.f;
+    float pg0 = 0.f, pg1 = 0.f;
+    auto tap = [&](int m0, int i) {
+        int d = n0 - m0 - (kAM - 1) + S * i;   // |d| < nt + 2*kAN: int suffices
+        d %= nt;
+        if (d < 0) d += nt;
+        return g[d];
+    };
     auto load = [&](int m0) {
         const int m = m0 + smm;
 #pragma unroll
@@ -81,21 +98,19 @@ __global__ void __launch_bounds__(kAW * 32, 2) k_analytic(float* __restrict__ ou
             const long long t = tb + stt + (kAW * 32 / kAM) * q;
             pf[q] = (t < ntr && m < nt) ? out[2 * (t * nt + m)] : 0.f;
         }
-        if (threadIdx.x < kAG) {
-            int d = n0 - m0 - (kAM - 1) + (int)threadIdx.x;   // |d| < nt + kAN: int suffices
-            d %= nt;
-            if (d < 0) d += nt;
-            pg = g[d];
+        if (threadIdx.x < 2 * kP) {
+            pg0 = tap(m0, 2 * pe + pa);
+            pg1 = tap(m0, 2 * pe + pa + 1);
         }
     };
     auto store = [&](int buf) {
 #pragma unroll
         for (int q = 0; q < kAQ; ++q) xs[buf][stt + (kAW * 32 / kAM) * q][smm] = pf[q];
-        if (threadIdx.x < kAG) gs[buf][threadIdx.x] = pg;
+        if (threadIdx.x < 2 * kP) tp[buf][pa][pe] = make_float2(pg0, pg1);
     };
-    float acc0[kAB], acc1[kAB];
+    float2 A0[kH], A1[kH];   // (output 2j, output 2j+1) of each trace
 #pragma unroll
-    for (int b = 0; b < kAB; ++b) acc0[b] = acc1[b] = 0.f;
+    for (int j = 0; j < kH; ++j) A0[j] = A1[j] = make_float2(0.f, 0.f);
     load(0);
     store(0);
     __syncthreads();
@@ -103,25 +118,37 @@ __global__ void __launch_bounds__(kAW * 32, 2) k_analytic(float* __restrict__ ou
     for (int m0 = 0; m0 < nt; m0 += kAM) {
         const bool more = m0 + kAM < nt;
         if (more) load(m0 + kAM);
-        // step k of this stage is input m0 + par + S*k; G[q] = gp[S*q] with
-        // q in [-(kAM/S - 1), kAB - 1], inside gs for every warp
+        // step k of this stage is input m0 + par + S*k.  Even steps k = 2u use
+        // the pairs starting at cw - 2u + 2j (alignment cw & 1), odd steps
+        // k = 2u + 1 those at cw - 2u - 1 + 2j; both index ranges lie inside
+        // tp for every warp (cw - k >= 0, cw + kAB <= 2*kP)
         const float* x0 = &xs[buf][lane][par];
         const float* x1 = &xs[buf][lane + 32][par];
-        const float* gp = &gs[buf][nb - n0 - par + kAM - 1];
-        float wr[kAB];   // wr[q & (kAB-1)] = G[q] for the kAB live q
+        const float2* pE = &tp[buf][cw & 1][cw >> 1];
+        const float2* pO = &tp[buf][(cw & 1) ^ 1][(cw - 1) >> 1];
+        float2 RE[kH], RO[kH];   // slot (j - u) & (kH-1) holds pair j of step 2u / 2u + 1
 #pragma unroll
-        for (int b = 1; b < kAB; ++b) wr[b] = gp[S * b];
+        for (int j = 1; j < kH; ++j) {
+            RE[j] = pE[j];
+            RO[j] = pO[j];
+        }
         for (int k0 = 0; k0 < kAM / S; k0 += kAB) {
+            const int u0 = k0 / 2;
 #pragma unroll
             for (int k = 0; k < kAB; ++k) {
+                const int u = k >> 1;
                 const int kk = k0 + k;
-                wr[(kAB - k) & (kAB - 1)] = gp[-S * kk];   // G[-kk] replaces G[kAB - kk]
+                if ((k & 1) == 0)
+                    RE[(kH - u) & (kH - 1)] = pE[-(u0 + u)];
+                else
+                    RO[(kH - u) & (kH - 1)] = pO[-(u0 + u)];
                 const float xv0 = x0[S * kk], xv1 = x1[S * kk];
+                const float2 X0 = make_float2(xv0, xv0), X1 = make_float2(xv1, xv1);
 #pragma unroll
-                for (int b = 0; b < kAB; ++b) {
-                    const float gv = wr[(b - k) & (kAB - 1)];
-                    acc0[b] = __fmaf_rn(xv0, gv, acc0[b]);
-                    acc1[b] = __fmaf_rn(xv1, gv, acc1[b]);
+                for (int j = 0; j < kH; ++j) {
+                    const float2 gv = (k & 1) ? RO[(j - u) & (kH - 1)] : RE[(j - u) & (kH - 1)];
+                    A0[j] = __ffma2_rn(X0, gv, A0[j]);
+                    A1[j] = __ffma2_rn(X1, gv, A1[j]);
                 }
             }
         }
@@ -135,9 +162,11 @@ __global__ void __launch_bounds__(kAW * 32, 2) k_analytic(float* __restrict__ ou
         const long long t = tb + lane + 32 * h;
         if (t >= ntr) continue;
 #pragma unroll
-        for (int b = 0; b < kAB; ++b) {
-            const int n = nb + S * b;
-            if (n < nt) out[2 * (t * nt + n) + 1] = h ? acc1[b] : acc0[b];
+        for (int j = 0; j < kH; ++j) {
+            const float2 v = h ? A1[j] : A0[j];
+            const int n = nb + S * 2 * j;
+            if (n < nt) out[2 * (t * nt + n) + 1] = v.x;
+            if (n + S < nt) out[2 * (t * nt + n + S) + 1] = v.y;
         }
     }
 }
