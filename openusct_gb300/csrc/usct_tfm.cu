@@ -26,6 +26,7 @@
 
 #include <cstdint>
 
+#include "usct_convert.cuh"
 #include "usct_gb300.h"
 
 int usct_internal_error(int code, const char* msg);   // usct_engine.cu
@@ -171,37 +172,8 @@ __global__ void __launch_bounds__(kAW * 32, 2) k_analytic(float* __restrict__ ou
     }
 }
 
-// Exact FP64 <-> FP32 conversions (IEEE round to nearest even) in integer
-// arithmetic: the hardware conversions issue to the FP64 pipe, of which this
-// part has very little.  Zeros and the normal range take the integer path;
-// subnormal, out-of-range, infinite and NaN values the hardware one.
-__device__ __forceinline__ float f64_to_f32(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-    const int e = (int)((b >> 52) & 0x7ff);
-    if (e >= 897 && e <= 1150) {   // FP32 exponent e - 896 in [1, 254]
-        const unsigned long long m = b & 0xfffffffffffffULL;
-        unsigned r = ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29);
-        const unsigned rem = (unsigned)(m & 0x1fffffffULL);   // the 29 dropped bits
-        r += (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;
-        return __uint_as_float(r | sign);   // a carry into the exponent is exact (to inf at the top)
-    }
-    if ((b << 1) == 0) return __uint_as_float(sign);
-    return __double2float_rn(x);
-}
-
-__device__ __forceinline__ double f32_to_f64(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xffu;
-    if (e - 1u < 254u) {
-        const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                     ((unsigned long long)(e + 896u) << 52) |
-                                     ((unsigned long long)(u & 0x7fffffu) << 29);
-        return __longlong_as_double((long long)b);
-    }
-    if ((u << 1) == 0) return __longlong_as_double((long long)((unsigned long long)u << 32));
-    return (double)f;
-}
+using usct_cvt::f32_to_f64;
+using usct_cvt::f64_to_f32;
 
 // out[i][j][m] = (data[i][m][j], 0): the Dataset layout to trace-major, each
 // FP64 sample converted to FP32 once.  32 x 32 tiles (m, j) through shared

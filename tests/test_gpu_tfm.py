@@ -60,6 +60,30 @@ def test_analytic_signal_matches_scipy(shape):
     assert err < 1e-5, err
 
 
+def test_analytic_real_part_rounds_like_numpy():
+    """The FP64 -> FP32 conversion of the samples (integer arithmetic on the
+    device) equals NumPy's round-to-nearest-even for ties, overflow, the
+    subnormal range, signed zeros, infinities and NaN."""
+    from openusct_gb300.imaging import analytic_signal
+    f = np.float32
+    one = 1.0
+    vals = [0.0, -0.0, one + 2.0 ** -24, one + 3 * 2.0 ** -24, -(one + 2.0 ** -24),
+            2.0 ** -23 * 3 + 1, float(np.finfo(f).max) * (1 + 2.0 ** -25),
+            float(np.finfo(f).max) * (1 + 2.0 ** -24), float(np.finfo(f).max),
+            2.0 ** -126, 2.0 ** -126 * (1 - 2.0 ** -25), 2.0 ** -140, 2.0 ** -149,
+            2.0 ** -150, 2.0 ** -151, 1e-300, -1e-300, 1e300, -1e300, np.inf, -np.inf, np.nan,
+            1.0000000596046448, 16777217.0, -16777219.0, 3.4e38, 1.1754942e-38]
+    rng = np.random.default_rng(4)
+    vals += list(rng.standard_normal(37) * 10.0 ** rng.integers(-40, 40, 37))
+    x = np.array(vals, np.float64).reshape(1, -1, 1)
+    with np.errstate(over="ignore"):
+        want = x.astype(np.float32).ravel()
+    got = analytic_signal(x).real.cpu().numpy().ravel()
+    nan = np.isnan(want)
+    assert np.array_equal(np.isnan(got), nan)
+    assert np.array_equal(got[~nan].view(np.uint32), want[~nan].view(np.uint32))
+
+
 @pytest.mark.parametrize("name", ["tfm2d", "tfm3d"])
 def test_tfm_matches_reference(name):
     from openusct_gb300.imaging import tfm
