@@ -375,9 +375,13 @@ def main():
         return
 
     desc_w, build_prob, C0, k0, mode = WORKLOADS[args.workload]
-    if args.n or args.nt:
+    if args.workload == "gn3d" and args.nt and not args.n:
+        # a shortened time axis (launch lists under ncu)
+        prob = problems.gn3d(seed=0, nt=args.nt)
+        desc_w = f"nt={prob.nt} variant of: " + desc_w
+    elif args.n or args.nt:
         if args.workload != "grad3d":
-            raise SystemExit("--n/--nt overrides apply to the grad3d workload only")
+            raise SystemExit("--n/--nt overrides apply to grad3d (and --nt to gn3d) only")
         n = args.n or 192
         prob = problems.cylinder3d(seed=0, n=n, h=0.2e-3 * 191 / (n - 1), nt=args.nt or 2000)
         desc_w = f"{n}^3 nt={prob.nt} variant of: " + desc_w

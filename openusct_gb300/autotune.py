@@ -86,7 +86,8 @@ def _synthetic(shape, nt):
 
 
 def time_kernels(shape, C, nt, tile, what=("fwd", "adj"), reps=2):
-    """Per-launch milliseconds of the forward and adjoint stencils for a tile."""
+    """Per-launch milliseconds of the forward, Born-forward and adjoint stencils
+    for a tile (``what`` names those timed: "fwd", "born", "adj")."""
     import torch
     from .backend import Plan, _ptr, _stream
     geom, m, h, dt, wav = _synthetic(shape, nt)
@@ -103,10 +104,14 @@ def time_kernels(shape, C, nt, tile, what=("fwd", "adj"), reps=2):
     md = torch.from_numpy(m).to(dev)
     wd = torch.from_numpy(wav).to(dev)
     mws = torch.empty(plan.model_bytes(), dtype=torch.uint8, device=dev)
-    mode = _lib.MODE_GRADIENT if "adj" in what else _lib.MODE_FORWARD
+    mode = (_lib.MODE_BORN if "born" in what else
+            _lib.MODE_GRADIENT if "adj" in what else _lib.MODE_FORWARD)
     bws = torch.empty(plan.batch_bytes(mode), dtype=torch.uint8, device=dev)
     s = _stream()
-    _lib.check(lib.usct_model_prepare(plan.handle, _ptr(mws), _ptr(md), None, None, _ptr(wd), s))
+    # a Born perturbation (1 % of m, smooth) when the Born sweep is timed
+    vd = (0.01 * md).contiguous() if "born" in what else None
+    _lib.check(lib.usct_model_prepare(plan.handle, _ptr(mws), _ptr(md), None, _ptr(vd), _ptr(wd),
+                                      s))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     out = {}
     ts = torch.cuda.current_stream()
@@ -121,6 +126,15 @@ def time_kernels(shape, C, nt, tile, what=("fwd", "adj"), reps=2):
         e1.record(ts)
         torch.cuda.synchronize()
         out["fwd_ms"] = e0.elapsed_time(e1) / (reps * (nt - 1))
+    if "born" in what:
+        # background and Born fields in lockstep: nt-1 launches of the Born stencil
+        e0.record(ts)
+        for _ in range(reps):
+            _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), 0,
+                                              _lib.MODE_BORN, None, s))
+        e1.record(ts)
+        torch.cuda.synchronize()
+        out["born_ms"] = e0.elapsed_time(e1) / (reps * (nt - 1))
     if "adj" in what:
         _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), 0,
                                           _lib.MODE_GRADIENT, None, s))
@@ -139,6 +153,10 @@ def time_kernels(shape, C, nt, tile, what=("fwd", "adj"), reps=2):
         out["fwd_GBs"] = (12 * C + 4) * cells / (out["fwd_ms"] * 1e-3) / 1e9
     if "adj_ms" in out:
         out["adj_GBs"] = (16 * C + 20) * cells / (out["adj_ms"] * 1e-3) / 1e9
+    if "born_ms" in out:
+        # the plan is one checkpoint segment, so every Born launch also writes
+        # the background's d2p stash (the last segment's): 24 C + 8 + 4 C
+        out["born_GBs"] = (28 * C + 8) * cells / (out["born_ms"] * 1e-3) / 1e9
     plan.check()
     out["tile"] = [plan.info("tile_x"), plan.info("tile_y"), plan.info("zchunk"),
                    plan.info("variant")] + [int(v) for v in tile[4:6]]
