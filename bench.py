@@ -484,9 +484,10 @@ def main():
     fwd_bytes = (12 * C + 4) * cells
     achieved = fwd_bytes / t_launch / 1e9
     # DRAM traffic of the same kernel from the committed ncu capture of a smaller
-    # case (128^3, 16 shots), scaled by cell-channels to this launch
+    # case (128^3, 32 shots: the same template instance), scaled by
+    # cell-channels to this launch
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "k_forward_tma_128cube_C16.md")
+    prof = os.path.join(ROOT, "profiles", "k_forward_tma_128cube_C32.md")
     if os.path.exists(prof):
         try:
             kv = {}
@@ -604,8 +605,8 @@ def main():
                          "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind,
                          "traffic": traffic,
-                         "traffic_source": "profiles/k_forward_tma_128cube_C16.md, scaled by "
-                                           "cell-channels (128^3x16 -> this launch)",
+                         "traffic_source": "profiles/k_forward_tma_128cube_C32.md, scaled by "
+                                           "cell-channels (128^3x32 -> this launch)",
                          "algorithmic_bytes_per_launch": fwd_bytes,
                          "launch_ms": t_launch * 1000.0},
             "pipeline_roofline": {"bytes_per_step": pipeline_bytes,
