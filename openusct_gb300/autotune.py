@@ -6,7 +6,7 @@ short forward sweep and one short backward sweep of each candidate with CUDA
 events and keeping the fastest.  Results are cached in a JSON file
 (``$OPENUSCT_GB300_CACHE`` or ``~/.cache/openusct_gb300/autotune.json``).
 
-It is also the driver for per-kernel profiling::
+It is also the entry point for per-kernel profiling::
 
     python -m openusct_gb300.autotune --n 128 --batch 16 --nt 24 --what fwd --tiles 64x4x0x1
 

@@ -1,6 +1,6 @@
 """CPU oracle for the ringfwi acoustic hot path -- TEST INFRASTRUCTURE ONLY.
 
-Only ``tests/``, ``__graft_entry__.smoke()`` (as the checker) and ``bench.py``'s
+Only ``tests/``, ``__graft_entry__.smoke()`` (to check the GPU result) and ``bench.py``'s
 CPU-baseline leg import this package.  The product (``openusct_gb300``) never
 does: it has no CPU fallback.
 
