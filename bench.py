@@ -21,7 +21,9 @@ sampled during the timed region and the number of kernels launched.
 Other workloads (not the default line): --workload ring2d (the 2D 256^2 ring,
 all 64 shots per launch), gn3d (the 224^3 Gauss-Newton Hessian-vector product),
 grad3d_large (320^3, 512 shots, 8 per launch), tfm2d (the TFM image of a
-64 x 1500 x 64 FMC).
+64 x 1500 x 64 FMC), invert2d (iterations of the device-resident inversion
+loop on the 2D ring).  --misfit gcn and --windows run the gradient workloads
+with the GCN misfit and with P-arrival data windows.
 """
 
 from __future__ import annotations
@@ -120,7 +122,7 @@ class Clocks:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_gradient_sample(prob, shot, nt_sample, k, mode="grad"):
+def cpu_gradient_sample(prob, shot, nt_sample, k, mode="grad", misfit="l2"):
     """Time the FP64 oracle gradient (or Gauss-Newton product) for one shot over
     nt_sample levels and scale to the full time axis: (shots/s, seconds, text)."""
     import numpy as np
@@ -139,7 +141,7 @@ def cpu_gradient_sample(prob, shot, nt_sample, k, mode="grad"):
     rec_all = oracle.forward_fmc(prob.m_true, geom, wav, prob.dt, prob.h, nt_sample, None, [shot])
     t0 = time.perf_counter()
     oracle.misfit_and_gradient(prob.m0, geom, wav, prob.dt, prob.h, nt_sample, rec_all, None,
-                               [shot], k=k)
+                               [shot], k=k, misfit_type=misfit)
     dt_s = time.perf_counter() - t0
     per_shot = dt_s * (prob.nt - 1) / (nt_sample - 1)
     grid = "x".join(str(v) for v in prob.shape)
@@ -223,6 +225,79 @@ def run_reference(args, prob, desc_w, mode):
                              "sample": desc},
             "e2e": {"value": value, "unit": "shots/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+INVERT_WORKLOAD = ("FWI inversion loop (fwi.invert: steepest descent on the Gaussian-smoothed "
+                   "gradient, backtracking line search), 2D 256^2 ring, dx=0.15mm, 64 elements, "
+                   "two seeded discs, nt=1500, L2, model and gradient kept on the GPU")
+
+
+def bench_invert(args):
+    """--workload invert2d: iterations/s of the device-resident fwi.invert
+    (openusct_gb300.invert.invert, fwi.py:535-660) on the 2D ring problem; one
+    step = one iteration: the gradient over all 64 shots, its smoothing and
+    scaling, and the line search's trial misfits."""
+    import numpy as np
+    import torch
+    from openusct_gb300 import backend, problems
+    from openusct_gb300.invert import invert
+
+    prob = problems.ring2d(seed=0)
+    dev = torch.device("cuda", 0)
+    geo = (prob.geom, prob.wavelet, prob.dt, prob.h, prob.nt)
+    dobs_h = backend.forward_fmc(prob.m_true, *geo)
+    dobs_d = torch.from_numpy(np.asarray(dobs_h, np.float32)).to(dev)
+    m0_d = torch.from_numpy(prob.m0).to(dev)
+    invert(m0_d, *geo, dobs_d, n_iter=max(3, args.warmup))
+    s = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        torch.cuda.synchronize()
+        ev0.record(s)
+        _m, hist = invert(m0_d, *geo, dobs_d, n_iter=args.steps)
+        ev1.record(s)
+        torch.cuda.synchronize()
+    t_ms = ev0.elapsed_time(ev1) / args.steps
+    # end to end: the same call with host arrays (the model, data and wavelet
+    # go up once per call, the model comes back)
+    t0 = time.perf_counter()
+    m_h, _ = invert(prob.m0, *geo, dobs_h, n_iter=args.steps)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    h2d = prob.m0.nbytes + np.asarray(dobs_h).nbytes + prob.wavelet.nbytes
+    cpu = None
+    if not args.no_cpu:
+        try:
+            import oracle
+            from oracle import invert as oinv
+            oracle.build()
+            sub = [0, 16, 32, 48]
+            t0 = time.perf_counter()
+            oinv.invert(prob.m0, *geo, np.asarray(dobs_h)[sub], src_list=sub, n_iter=1,
+                        backend=oinv.FP64Backend())
+            secs = time.perf_counter() - t0
+            cpu = {"value": len(sub) / 64.0 / secs, "unit": "iterations/s",
+                   "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+                   "kind": "port",
+                   "sample": "1 iteration of the host restatement of fwi.invert (oracle/invert.py, "
+                             "FP64 C core) with 4 of the 64 shots, scaled by 16",
+                   "seconds": secs}
+        except Exception as exc:  # reported, never required
+            cpu = {"value": None, "error": str(exc)[:200]}
+    line = {"metric": "FWI iterations/s (device-resident invert)", "value": 1000.0 / t_ms,
+            "unit": "iterations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (two seeded discs; the data from the true model on the GPU)",
+            "config": {"workload": INVERT_WORKLOAD, "grid": list(prob.shape), "nt": prob.nt,
+                       "shots": 64, "l2": "three wavefield levels of all 64 shots (50 MB) fit "
+                                         "in L2"},
+            "misfit_history": [float(v) for v in hist],
+            "e2e": {"value": 1.0 / e2e_s, "unit": "iterations/s",
+                    "h2d_bytes_per_step": int(h2d / args.steps),
+                    "d2h_bytes_per_step": int(m_h.nbytes / args.steps),
+                    "api": "openusct_gb300.invert.invert"},
+            "cpu_baseline": cpu, "clocks": clk.summary()}
     print(json.dumps(line))
 
 
@@ -350,11 +425,16 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="grad3d", choices=sorted(WORKLOADS) + ["tfm2d"])
+    ap.add_argument("--workload", default="grad3d",
+                    choices=sorted(WORKLOADS) + ["tfm2d", "invert2d"])
     ap.add_argument("--n", type=int, default=0, help="override the grid size (smaller variants)")
     ap.add_argument("--nt", type=int, default=0, help="override the time levels")
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--ckpt", type=int, default=-1)
+    ap.add_argument("--misfit", default="l2", choices=["l2", "gcn"],
+                    help="gradient workloads: the misfit (L2 or GCN, libuap.hpp:125-162)")
+    ap.add_argument("--windows", action="store_true",
+                    help="gradient workloads: P-arrival data windows as time_weights")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
@@ -366,12 +446,12 @@ def main():
     import numpy as np
     from openusct_gb300 import problems
 
-    if args.workload == "tfm2d":
+    if args.workload in ("tfm2d", "invert2d"):
         if args.impl == "reference" or rank != 0:
             return
         import torch
         torch.cuda.set_device(0)
-        bench_tfm(args)
+        (bench_tfm if args.workload == "tfm2d" else bench_invert)(args)
         return
 
     desc_w, build_prob, C0, k0, mode = WORKLOADS[args.workload]
@@ -430,11 +510,24 @@ def main():
     J = torch.zeros(C, dtype=torch.float64, device=dev)
     g = torch.empty(prob.shape, dtype=torch.float64, device=dev)
     vt = torch.from_numpy(prob.v).to(dev) if mode == "gn" else None
+    # the f1 options: GCN misfit and P-arrival windows (fwi.p_window_weights) as
+    # time_weights, both through the windowed entry point
+    mt = 1 if args.misfit == "gcn" else 0
+    tw = None
+    if args.windows and mode == "grad":
+        from openusct_gb300 import imaging
+        tw = imaging.p_window_weights(dobs, prob.dt, prob.f0, as_tensor=True).float().contiguous()
+    variant = mode == "grad" and (mt != 0 or tw is not None)
+    tw_p = P(tw) if tw is not None else ctypes.c_void_p(0)
 
     def step():
         if mode == "gn":
             _lib.check(lib.usct_gn_hessian_vector_dev(plan.handle, P(m0), None, P(wav), P(vt),
                                                       P(g), None, P(mws), P(bws), sp))
+        elif variant:
+            _lib.check(lib.usct_misfit_and_gradient_tw_dev(plan.handle, P(m0), None, P(wav),
+                                                           P(dobs), tw_p, mt, P(J), P(g), P(mws),
+                                                           P(bws), sp))
         else:
             _lib.check(lib.usct_misfit_and_gradient_dev(plan.handle, P(m0), None, P(wav),
                                                         P(dobs), P(J), P(g), P(mws), P(bws), sp))
@@ -508,10 +601,12 @@ def main():
     m0_h = prob.m0
     dobs_h = dobs.double().cpu().numpy()
     kw = dict(src_list=shots, batch=C, ckpt_k=ckpt or None)
+    tw_h = tw.cpu().numpy() if tw is not None else None
     call = (lambda: backend.gn_hessian_vector(m0_h, prob.geom, prob.wavelet, prob.dt, prob.h,
                                               prob.nt, prob.v, **kw)) if mode == "gn" else \
         (lambda: backend.misfit_and_gradient(m0_h, prob.geom, prob.wavelet, prob.dt, prob.h,
-                                             prob.nt, dobs_h, **kw)[1])
+                                             prob.nt, dobs_h, misfit_type=args.misfit,
+                                             time_weights=tw_h, **kw)[1])
     call()   # first call builds the plan (and, for small grids, captures graphs)
     ne = 1 if cells * C > (1 << 24) else 5
     if world > 1:
@@ -526,6 +621,8 @@ def main():
         te = float(tt.item())
     h2d = m0_h.nbytes + prob.wavelet.nbytes + (prob.v.nbytes if mode == "gn" else
                                                 C * prob.nt * plan.n_rx * 4)
+    if tw_h is not None:
+        h2d += tw_h.nbytes
     e2e = {"value": C * world / te, "unit": "shots/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(gh.nbytes + (0 if mode == "gn" else 8 * C)),
            "api": "openusct_gb300.backend." + ("gn_hessian_vector" if mode == "gn"
@@ -534,18 +631,19 @@ def main():
 
     # plain one-shot-per-launch GPU form, same workload, one shot
     plain = None
-    if rank == 0 and not args.no_plain and mode == "grad":
+    no_plain = args.no_plain or variant   # the plain form is the reference's L2 GPU path
+    if rank == 0 and not no_plain and mode == "grad":
         backend._PLANS.clear()
         torch.cuda.empty_cache()
         tx1, rx1 = element_csr(prob.geom, prob.shape, [0], None)
         pplan = backend.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx1, rx1, batch=1)
         need = pplan.plain_bytes(True)
         free = torch.cuda.mem_get_info(dev)[0]
-    if rank == 0 and not args.no_plain and mode == "grad" and need > 0.95 * free:
+    if rank == 0 and not no_plain and mode == "grad" and need > 0.95 * free:
         plain = {"value": None, "unit": "shots/s",
                  "infeasible": f"the plain form keeps the full FP32 history: {need / 2**30:.0f} GiB "
                                f"> {free / 2**30:.0f} GiB free HBM"}
-    elif rank == 0 and not args.no_plain and mode == "grad":
+    elif rank == 0 and not no_plain and mode == "grad":
         pws = torch.empty(pplan.plain_bytes(True), dtype=torch.uint8, device=dev)
         J1 = torch.zeros(1, dtype=torch.float64, device=dev)
         d1 = dobs[0:1].contiguous()
@@ -562,7 +660,7 @@ def main():
         del pws
 
     serve = None
-    if rank == 0 and not args.no_serve and args.workload == "grad3d":
+    if rank == 0 and not args.no_serve and args.workload == "grad3d" and not variant:
         try:
             serve = serve_phase(args)
         except Exception as exc:   # reported, never fatal for the main line
@@ -574,7 +672,9 @@ def main():
             import oracle
             oracle.build()
             v, secs, desc = cpu_gradient_sample(prob, 0, 40 if len(prob.shape) == 3 else 600, 8,
-                                                mode)
+                                                mode, args.misfit)
+            if tw is not None:
+                desc += "; without the data windows (an elementwise product of the residual)"
             cpu = {"value": v, "unit": "shots/s",
                    "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
                    "kind": "port", "sample": desc, "seconds": secs}
@@ -598,6 +698,9 @@ def main():
                                                               plan.info("tile_y"),
                                                               plan.info("zchunk")],
                        "parallelism": f"replicas{world}" if world > 1 else "single",
+                       "misfit": args.misfit if mode == "grad" else None,
+                       "time_weights": ("P-arrival windows (imaging.p_window_weights)"
+                                        if tw is not None else None),
                        "l2": l2_note},
             "grid_updates_per_s": value * cells * (prob.nt - 1),
             "roofline": {"bound": "hbm",
