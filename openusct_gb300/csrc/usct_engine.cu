@@ -29,6 +29,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "usct_convert.cuh"
 #include "usct_gb300.h"
 #include "usct_kernels.cuh"
 #include "usct_tma.cuh"
@@ -564,51 +565,80 @@ __global__ void k_adjsrc(const float* __restrict__ adj, float* res, int C, int n
 }
 
 // GCN adjoint source (libuap.hpp:133-162, fwi.py:158-167) from the traces in
-// res ([nt][n_rx][C]), in place: per (receiver j, shot c) FP64 sums over time
-// of the FP32 traces; gj[j][c] = 1 - c_j for the per-shot misfit.  With a
-// window tw the traces in res are already windowed, dobs is windowed here and
-// the adjoint source is multiplied by the window (fwi.py:298-301).
-__global__ void k_gcn(float* res, const float* __restrict__ dobs, int C, int logC, int nt, int nrx,
-                      int shot0, int nb, double* gj, const float* __restrict__ tw) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= nrx * C) return;
+// res ([nt][n_rx][C]), in place, for each (receiver j, shot c):
+//   sn = sqrt(sum sv^2) + eps, on = sqrt(sum ov^2) + eps,
+//   c_j = sum sv*ov / (sn*on)   (= sum (sv/sn)(ov/on), the reference's form),
+//   adj = a*ov + b*sv with a = -1/(on*sn), b = c_j/(sn*sn)
+//         (= -(ov/on - c_j*sv/sn)/sn, the reference's form),
+// and gj[j][c] = 1 - c_j for the per-shot misfit.  The sums are FP64 over the
+// FP32 traces, each accumulated with fused multiply-adds over kGS contiguous
+// time slices and the slices added in order -- no division per sample (the
+// FP64 pipe is small on this part).  Block (32, kGS): lane x owns the trace
+// idx = 32*blockIdx.x + x (idx = j*C + c), row y one time slice; the lanes of
+// a warp read 32 consecutive floats of a time level.  With a window tw the
+// traces in res are already windowed, dobs is windowed here and the adjoint
+// source is multiplied by the window (fwi.py:298-301).
+constexpr int kGS = 8;
+__global__ void __launch_bounds__(32 * kGS) k_gcn(float* res, const float* __restrict__ dobs, int C,
+                                                  int logC, int nt, int nrx, int shot0, int nb,
+                                                  double* gj, const float* __restrict__ tw) {
+    __shared__ double part[kGS][32][3];
+    __shared__ double coef[32][2];
+    const int x = threadIdx.x, y = threadIdx.y;
+    const int idx = blockIdx.x * 32 + x;
+    const bool live = idx < nrx * C;
     const int j = idx >> logC, c = idx & (C - 1);
-    float* col = res + (long long)j * C + c;
+    const bool shot = live && c < nb;
     const long long rstride = (long long)nrx * C;
-    if (c >= nb) {
-        for (int n = 0; n < nt; ++n) col[n * rstride] = 0.f;
-        gj[idx] = 0.0;
-        return;
-    }
-    const float* ob = dobs + (long long)(shot0 + c) * nt * nrx + j;
-    const float* wb = tw ? tw + (long long)(shot0 + c) * nt * nrx + j : nullptr;
+    float* col = res + (long long)j * C + c;
+    const int L = (nt + kGS - 1) / kGS;
+    const int n0 = min(nt, y * L), n1 = min(nt, n0 + L);
+    const float* ob = shot ? dobs + (long long)(shot0 + c) * nt * nrx + j : nullptr;
+    const float* wb = (shot && tw) ? tw + (long long)(shot0 + c) * nt * nrx + j : nullptr;
     auto obs = [&](int n) -> double {
         const long long o = (long long)n * nrx;
-        return wb ? (double)(ob[o] * wb[o]) : (double)ob[o];
+        return usct_cvt::f32_to_f64(wb ? ob[o] * wb[o] : ob[o]);
     };
-    const double eps = 1e-12;
-    double sn = 0.0, on = 0.0;
-    for (int n = 0; n < nt; ++n) {
-        const double sv = (double)col[n * rstride];
-        const double ov = obs(n);
-        sn += sv * sv;
-        on += ov * ov;
+    double ss = 0.0, oo = 0.0, so = 0.0;
+    if (shot) {
+        for (int n = n0; n < n1; ++n) {
+            const double sv = usct_cvt::f32_to_f64(col[n * rstride]);
+            const double ov = obs(n);
+            ss = fma(sv, sv, ss);
+            oo = fma(ov, ov, oo);
+            so = fma(sv, ov, so);
+        }
     }
-    sn = sqrt(sn) + eps;
-    on = sqrt(on) + eps;
-    double cc = 0.0;
-    for (int n = 0; n < nt; ++n) {
-        const double sv = (double)col[n * rstride];
-        const double ov = obs(n);
-        cc += (sv / sn) * (ov / on);
+    part[y][x][0] = ss;
+    part[y][x][1] = oo;
+    part[y][x][2] = so;
+    __syncthreads();
+    if (y == 0 && live) {
+        double S = 0.0, O = 0.0, D = 0.0;
+        for (int q = 0; q < kGS; ++q) {
+            S += part[q][x][0];
+            O += part[q][x][1];
+            D += part[q][x][2];
+        }
+        const double eps = 1e-12;
+        const double sn = sqrt(S) + eps, on = sqrt(O) + eps;
+        const double cc = D / (sn * on);
+        coef[x][0] = -1.0 / (on * sn);
+        coef[x][1] = cc / (sn * sn);
+        gj[idx] = shot ? 1.0 - cc : 0.0;
     }
-    for (int n = 0; n < nt; ++n) {
-        const double sv = (double)col[n * rstride];
-        const double ov = obs(n);
-        const float adj = (float)(-(ov / on - cc * (sv / sn)) / sn);
+    __syncthreads();
+    if (!live) return;
+    if (!shot) {
+        for (int n = n0; n < n1; ++n) col[n * rstride] = 0.f;
+        return;
+    }
+    const double A = coef[x][0], B = coef[x][1];
+    for (int n = n0; n < n1; ++n) {
+        const double sv = usct_cvt::f32_to_f64(col[n * rstride]);
+        const float adj = usct_cvt::f64_to_f32(fma(A, obs(n), B * sv));
         col[n * rstride] = wb ? adj * wb[(long long)n * nrx] : adj;
     }
-    gj[idx] = 1.0 - cc;
 }
 
 __global__ void k_gcn_j(const double* __restrict__ gj, int C, int nrx, int shot0, int nb, double* J) {
@@ -1093,8 +1123,8 @@ extern "C" int usct_batch_misfit_tw(usct_plan* p, void* batch_ws, int b, const f
     const int shot0 = b * p->C;
     const int nb = std::min(p->C, p->n_tx - shot0);
     const int n = p->n_rx * p->C;
-    k_gcn<<<(n + 127) / 128, 128, 0, s>>>(B.res, dobs, p->C, p->logC, p->nt, p->n_rx, shot0, nb, B.gj,
-                                          weights);
+    k_gcn<<<(n + 31) / 32, dim3(32, kGS), 0, s>>>(B.res, dobs, p->C, p->logC, p->nt, p->n_rx, shot0,
+                                                  nb, B.gj, weights);
     ++p->launches;
     if (J) {
         k_gcn_j<<<1, 64, 0, s>>>(B.gj, p->C, p->n_rx, shot0, nb, J);

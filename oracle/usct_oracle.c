@@ -727,34 +727,44 @@ static int grad32_impl(const double* m, const int* dims, int ndim, double h, dou
             /* windows as the device applies them: FP32 products with the FP32 window */
             const double* W = tw ? tw + (size_t)t * nt * nrx : NULL;
             if (!born_v && misfit_type == 1) {
-                /* GCN as the device computes it: per receiver, FP64 sums over time of
-                 * the FP32 traces (sequential in n), J = sum_j (1 - c_j) in j order */
+                /* GCN as the device computes it (k_gcn): per receiver, FP64 sums over
+                 * time of the FP32 traces, each with fused multiply-adds over KGS
+                 * contiguous time slices and the slices added in order;
+                 * c_j = sum sv*ov / (sn*on); adj = a*ov + b*sv with a = -1/(on*sn),
+                 * b = c_j/(sn*sn) (the reference's -(ov/on - c_j*sv/sn)/sn);
+                 * J = sum_j (1 - c_j) in j order */
                 const double* ob = dobs + (size_t)t * nt * nrx;
                 if (W)
                     for (size_t z = 0; z < (size_t)nt * nrx; ++z) dsyn[z] = dsyn[z] * (float)W[z];
 #define OBS(z) (W ? (double)((float)ob[(z)] * (float)W[(z)]) : (double)(float)ob[(z)])
                 const double eps = 1e-12;
+                const int KGS = 8;
+                const int L = (nt + KGS - 1) / KGS;
                 double J = 0.0;
                 for (int j = 0; j < nrx; ++j) {
-                    double sn = 0.0, on = 0.0, cc = 0.0;
-                    for (int n = 0; n < nt; ++n) {
-                        const double sv = (double)dsyn[(size_t)n * nrx + j];
-                        const double ov = OBS((size_t)n * nrx + j);
-                        sn += sv * sv;
-                        on += ov * ov;
+                    double S = 0.0, O = 0.0, D = 0.0;
+                    for (int q = 0; q < KGS; ++q) {
+                        const int n0 = q * L < nt ? q * L : nt;
+                        const int n1 = n0 + L < nt ? n0 + L : nt;
+                        double ss = 0.0, oo = 0.0, so = 0.0;
+                        for (int n = n0; n < n1; ++n) {
+                            const double sv = (double)dsyn[(size_t)n * nrx + j];
+                            const double ov = OBS((size_t)n * nrx + j);
+                            ss = fma(sv, sv, ss);
+                            oo = fma(ov, ov, oo);
+                            so = fma(sv, ov, so);
+                        }
+                        S += ss;
+                        O += oo;
+                        D += so;
                     }
-                    sn = sqrt(sn) + eps;
-                    on = sqrt(on) + eps;
-                    for (int n = 0; n < nt; ++n) {
-                        const double sv = (double)dsyn[(size_t)n * nrx + j];
-                        const double ov = OBS((size_t)n * nrx + j);
-                        cc += (sv / sn) * (ov / on);
-                    }
+                    const double sn = sqrt(S) + eps, on = sqrt(O) + eps;
+                    const double cc = D / (sn * on);
+                    const double A = -1.0 / (on * sn), B = cc / (sn * sn);
                     for (int n = 0; n < nt; ++n) {
                         const size_t z = (size_t)n * nrx + j;
                         const double sv = (double)dsyn[z];
-                        const double ov = OBS(z);
-                        const float adj = (float)(-(ov / on - cc * (sv / sn)) / sn);
+                        const float adj = (float)fma(A, OBS(z), B * sv);
                         res[c][z] = W ? adj * (float)W[z] : adj;
                     }
                     J += 1.0 - cc;
