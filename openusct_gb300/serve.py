@@ -150,7 +150,7 @@ class GpuExecutor:
     def run(self, req, plan):
         torch = self.torch
         from .backend import (_check_misfit, _grid_array, _ptr, _stream, _time_weights,
-                              _wavelet)
+                              _to_dev, _wavelet)
         lib = plan._lib
         dev = self.device
         st = torch.cuda.Stream(device=dev)
@@ -184,7 +184,7 @@ class GpuExecutor:
                 raise ValueError(f"dobs must have shape {(plan.n_tx, plan.nt, plan.n_rx)}")
             mt = _check_misfit(req.misfit_type)
             tw = _time_weights(req.time_weights, plan, dev)
-            dobs = torch.from_numpy(np.ascontiguousarray(req.dobs, np.float32)).to(dev)
+            dobs = _to_dev(req.dobs, torch.float32, dev)
             bws = torch.empty(plan.batch_bytes(_lib.MODE_GRADIENT), dtype=torch.uint8, device=dev)
             J = torch.zeros(plan.n_tx, dtype=torch.float64, device=dev)
             g = torch.empty(plan.shape, dtype=torch.float64, device=dev)

@@ -103,3 +103,39 @@ def test_tfm_buffers_have_no_overrun():
     assert _intact(A, 8 * n_tx * n_rx * nt)
     assert _intact(re, 8 * npix ** 3) and _intact(im, 8 * npix ** 3)
     assert _intact(W, 8 * n_tx * nt * n_rx)
+
+
+def test_uploads_cast_on_the_device_equal_numpy_casts():
+    """Host arrays go up as they are and are cast on the device: the device
+    values equal NumPy's astype bit for bit (FP64 -> FP32 rounding with
+    overflow and subnormals, FP32 -> FP64 widening, ints, Fortran order), from
+    concurrent threads too."""
+    import threading
+    from openusct_gb300 import backend
+    rng = np.random.default_rng(3)
+    dev = torch.device("cuda", 0)
+    cases = [(rng.standard_normal((37, 129, 61)) * 10.0 ** rng.integers(-30, 30, (37, 129, 61)),
+              torch.float32, np.float32),
+             (rng.standard_normal(600001).astype(np.float32), torch.float64, np.float64),
+             (rng.integers(-1000, 1000, (700, 500)), torch.float32, np.float32),
+             (np.asfortranarray(rng.standard_normal((513, 1031))), torch.float32, np.float32)]
+    for a, td, nd in cases:
+        got = backend._to_dev(a, td, dev).cpu().numpy()
+        with np.errstate(over="ignore"):
+            want = np.ascontiguousarray(a, dtype=nd)
+        assert got.shape == want.shape
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    errs = []
+
+    def up(seed):
+        b = np.random.default_rng(seed).standard_normal((300, 1000))
+        for _ in range(5):
+            if not np.array_equal(backend._to_dev(b, torch.float32, dev).cpu().numpy(),
+                                  b.astype(np.float32)):
+                errs.append(seed)
+    ts = [threading.Thread(target=up, args=(s,)) for s in range(4)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errs
