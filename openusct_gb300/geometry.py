@@ -311,3 +311,31 @@ def ricker(nt, dt, f0, t0=None):
     t = np.arange(nt) * dt - t0
     a = (math.pi * f0 * t) ** 2
     return (1.0 - 2.0 * a) * np.exp(-a)
+
+
+def make_sponge(shape, width=25, strength=0.08):
+    """Multiplicative damping mask for the ``sponge=`` argument
+    (solver.make_sponge, simulation/ringfwi/solver.py:22-42): 1 in the
+    interior; on the k-th cell from an edge (k < width) of every axis the
+    factor exp(-(strength * (width - k))^2).  A 2D mask is the outer product
+    of the row and column profiles, equal to the reference's; for 3D grids the
+    three axis profiles multiply (the reference builds 2D masks only).  As in
+    the reference, an axis shorter than ``width`` is an error."""
+    shape = tuple(int(n) for n in shape)
+    if len(shape) not in (2, 3):
+        raise ValueError("make_sponge needs a 2D or 3D shape")
+    k = np.arange(width)
+    ramp = np.exp(-((strength * (width - k)) ** 2))
+
+    def axis(n):
+        if n < width or width < 1:
+            raise ValueError(f"axis of {n} cells cannot hold a {width}-cell sponge")
+        f = np.ones(n)
+        f[:width] = ramp
+        f[n - width:] = ramp[::-1]
+        return f
+
+    mask = np.outer(axis(shape[-2]), axis(shape[-1]))
+    if len(shape) == 3:
+        mask = axis(shape[0])[:, None, None] * mask[None, :, :]
+    return mask

@@ -250,3 +250,28 @@ def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
     path.write_text("{not json")
     assert autotune.lookup((64, 64, 64), 16) is None
     assert autotune._parse_tiles("64x4x0x1x6x4,32x8") == [(64, 4, 0, 1, 6, 4), (32, 8, 0)]
+
+
+def test_make_sponge_matches_the_reference_and_extends_to_3d():
+    import os
+    import sys
+    from openusct_gb300.geometry import make_sponge
+    m = make_sponge((64, 80), width=10, strength=0.1)
+    assert m.shape == (64, 80) and m[32, 40] == 1.0
+    assert np.allclose(m, m[::-1, ::-1]) and m.min() > 0.0 and m.max() == 1.0
+    assert m[0, 40] == np.exp(-((0.1 * 10) ** 2))
+    m3 = make_sponge((40, 64, 80), width=10, strength=0.1)
+    assert np.array_equal(m3[20], m) and m3.shape == (40, 64, 80)
+    assert np.array_equal(m3[:, 32, 40], make_sponge((40, 30), 10, 0.1)[:, 15])
+    for bad in ((8, 80), (64, 80, 5)):
+        with pytest.raises(ValueError):
+            make_sponge(bad, width=10)
+    ref = "/root/reference/simulation"
+    if os.path.isdir(ref):
+        sys.path.insert(0, ref)
+        try:
+            from ringfwi.solver import make_sponge as ref_sponge
+        finally:
+            sys.path.remove(ref)
+        for shape, w, s in (((64, 80), 10, 0.1), ((101, 101), 25, 0.08), ((50, 200), 20, 0.05)):
+            assert np.array_equal(make_sponge(shape, w, s), ref_sponge(shape, w, s))
