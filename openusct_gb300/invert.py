@@ -142,6 +142,85 @@ def _backend(backend):
     return gb
 
 
+class _Evaluator:
+    """``misfit`` / ``misfit_and_gradient`` of :mod:`openusct_gb300.backend`
+    for one inversion.  The data, wavelet, sponge and windows go up once.
+    When the acquisition is one shot batch, a line-search trial runs its
+    forward sweep in gradient mode (checkpoints and the last segment's stash)
+    and keeps it, so the gradient at the accepted trial model -- the next
+    iteration's first call -- only runs the backward sweep: the same engine
+    calls in the same order as ``usct_misfit_and_gradient_tw_dev`` (prepare,
+    forward, misfit, backward, finalize), so J and g are identical, and one
+    forward sweep per iteration is saved."""
+
+    def __init__(self, gb, m0, geom, wavelet, dt, h, nt, dobs, sponge, src_list, misfit_type,
+                 footprints, time_weights, batch=None):
+        self.gb = gb
+        self.mt = gb._check_misfit(misfit_type)
+        p = self.plan = gb._setup(m0, geom, h, dt, nt, src_list, footprints, _lib.MODE_GRADIENT,
+                                  batch, None, None)
+        dev = m0.device
+        self.wd = gb._wavelet(wavelet, nt, dev)
+        self.sd = gb._grid_array(sponge, tuple(m0.shape), "sponge", dev)
+        self.od = gb._to_dev(dobs, torch.float32, dev)
+        if tuple(self.od.shape) != (p.n_tx, p.nt, p.n_rx):
+            raise ValueError(f"dobs has shape {tuple(self.od.shape)}, expected "
+                             f"{(p.n_tx, p.nt, p.n_rx)}")
+        self.tw = gb._time_weights(time_weights, p, dev)
+        self.J = torch.zeros(p.n_tx, dtype=torch.float64, device=dev)
+        self.mws = p.workspace("model", p.model_bytes(), dev)
+        self.bws = p.workspace(_lib.MODE_GRADIENT, p.batch_bytes(_lib.MODE_GRADIENT), dev)
+        self.single = p.nbatch == 1
+        # the model tensor whose forward state the workspaces hold.  The
+        # caller must not change that tensor before asking for its gradient
+        # (the descent loop asks right after the accepted trial; the model
+        # updates write through the library, which torch's version counter
+        # does not see, so identity is the contract)
+        self.kept = None
+
+    def _forward_misfit(self, b, mode, s):
+        P, lib, h = self.gb._ptr, self.plan._lib, self.plan.handle
+        _lib.check(lib.usct_batch_forward(h, P(self.mws), P(self.bws), b, mode, None, s))
+        _lib.check(lib.usct_batch_misfit_tw(h, P(self.bws), b, P(self.od), P(self.tw), self.mt,
+                                            P(self.J), s))
+
+    def _prepare(self, m, s):
+        P = self.gb._ptr
+        _lib.check(self.plan._lib.usct_model_prepare(self.plan.handle, P(self.mws), P(m),
+                                                     P(self.sd), None, P(self.wd), s))
+
+    def misfit(self, m):
+        gb = self.gb
+        with self.plan.lock, gb._on_exec_stream() as st:
+            s = gb._stream(st)
+            self._prepare(m, s)
+            mode = _lib.MODE_GRADIENT if self.single else _lib.MODE_FORWARD
+            for b in range(self.plan.nbatch):
+                self._forward_misfit(b, mode, s)
+            self.plan.check(st)
+        self.kept = m if self.single else None
+        return float(np.sum(self.J.cpu().numpy()))
+
+    def misfit_and_gradient(self, m):
+        gb, P = self.gb, self.gb._ptr
+        lib, h = self.plan._lib, self.plan.handle
+        g = torch.empty(self.plan.shape, dtype=torch.float64, device=m.device)
+        reuse = self.kept is not None and self.kept is m
+        with self.plan.lock, gb._on_exec_stream() as st:
+            s = gb._stream(st)
+            if reuse:
+                _lib.check(lib.usct_batch_backward(h, P(self.mws), P(self.bws), 0, s))
+            else:
+                self._prepare(m, s)
+                for b in range(self.plan.nbatch):
+                    self._forward_misfit(b, _lib.MODE_GRADIENT, s)
+                    _lib.check(lib.usct_batch_backward(h, P(self.mws), P(self.bws), b, s))
+            _lib.check(lib.usct_model_gradient(h, P(self.mws), P(m), P(g), s))
+            self.plan.check(st)
+        self.kept = None
+        return float(np.sum(self.J.cpu().numpy())), g
+
+
 def invert(m0, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, n_iter=15,
            step_frac=0.02, update_mask=None, m_bounds=None, smooth_sigma=1.0, n_linesearch=8,
            verbose=False, backend=None, misfit_type="l2", footprints=None, progress=None,
@@ -187,12 +266,18 @@ def _descent(be, ops, m0, geom, wavelet, dt, h, nt, dobs, sponge, src_list, n_it
              footprints, time_weights):
     """fwi.py:623-660 on the device."""
     kw = dict(misfit_type=misfit_type, footprints=footprints, time_weights=time_weights)
+    from . import backend as gb
+    if be is gb and len(src_list) > 0:
+        ev = _Evaluator(gb, m0, geom, wavelet, dt, h, nt, dobs, sponge, src_list, misfit_type,
+                        footprints, time_weights)
+        mg, mf = ev.misfit_and_gradient, ev.misfit
+    else:
+        def mg(mm):
+            return be.misfit_and_gradient(mm, geom, wavelet, dt, h, nt, dobs, sponge, src_list,
+                                          **kw)
 
-    def mg(mm):
-        return be.misfit_and_gradient(mm, geom, wavelet, dt, h, nt, dobs, sponge, src_list, **kw)
-
-    def mf(mm):
-        return be.misfit(mm, geom, wavelet, dt, h, nt, dobs, sponge, src_list, **kw)
+        def mf(mm):
+            return be.misfit(mm, geom, wavelet, dt, h, nt, dobs, sponge, src_list, **kw)
 
     m = m0.clone()
     gm = ops.empty()

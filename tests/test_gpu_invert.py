@@ -107,6 +107,31 @@ def test_device_invert_equals_host_loop_and_reference(key):
     assert rel_l2(m - c["m0"], c["m_" + key] - c["m0"]) < 1e-3
 
 
+def test_evaluator_reuses_the_trial_forward_bit_exactly():
+    """The inversion's evaluator: a trial misfit followed by the gradient at
+    the same model (only the backward sweep runs) gives J and g bit-identical
+    to backend.misfit_and_gradient -- L2 and GCN, one shot batch (the forward
+    is kept) and several (it is not) -- and so does a gradient call without a
+    trial before it."""
+    import openusct_gb300.backend as gb
+    from openusct_gb300.invert import _Evaluator
+    c = load("invert2d")
+    dev = torch.device("cuda", 0)
+    m = torch.from_numpy(c["m0"]).to(dev)
+    for batch, mt in ((None, "l2"), (None, "gcn"), (1, "l2")):
+        ev = _Evaluator(gb, m, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"], None, c.src_list,
+                        mt, None, None, batch=batch)
+        assert ev.single == (batch is None)
+        Jr, gr = gb.misfit_and_gradient(m, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                                        src_list=c.src_list, misfit_type=mt, batch=batch)
+        Jt = ev.misfit(m)
+        J, g = ev.misfit_and_gradient(m)
+        assert Jt == Jr and J == Jr
+        assert torch.equal(g, gr)
+        J2, g2 = ev.misfit_and_gradient(m)
+        assert J2 == Jr and torch.equal(g2, gr)
+
+
 def test_device_invert_keeps_tensors_on_the_device():
     from openusct_gb300.invert import invert
     c = load("invert2d")
