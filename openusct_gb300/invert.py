@@ -168,8 +168,12 @@ class _Evaluator:
                              f"{(p.n_tx, p.nt, p.n_rx)}")
         self.tw = gb._time_weights(time_weights, p, dev)
         self.J = torch.zeros(p.n_tx, dtype=torch.float64, device=dev)
-        self.mws = p.workspace("model", p.model_bytes(), dev)
-        self.bws = p.workspace(_lib.MODE_GRADIENT, p.batch_bytes(_lib.MODE_GRADIENT), dev)
+        # workspaces of its own, not the plan's shared ones: the kept forward
+        # state must survive other calls on the same (cached) plan between
+        # a trial and its gradient
+        self.mws = torch.empty(max(p.model_bytes(), 256), dtype=torch.uint8, device=dev)
+        self.bws = torch.empty(max(p.batch_bytes(_lib.MODE_GRADIENT), 256), dtype=torch.uint8,
+                               device=dev)
         self.single = p.nbatch == 1
         # the model tensor whose forward state the workspaces hold.  The
         # caller must not change that tensor before asking for its gradient

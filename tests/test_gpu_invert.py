@@ -130,6 +130,17 @@ def test_evaluator_reuses_the_trial_forward_bit_exactly():
         assert torch.equal(g, gr)
         J2, g2 = ev.misfit_and_gradient(m)
         assert J2 == Jr and torch.equal(g2, gr)
+    # another call on the same (cached) plan between a trial and its gradient
+    # leaves the kept state alone
+    ev = _Evaluator(gb, m, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"], None, c.src_list,
+                    "l2", None, None)
+    Jr, gr = gb.misfit_and_gradient(m, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                                    src_list=c.src_list)
+    ev.misfit(m)
+    gb.misfit_and_gradient(m * 1.01, c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                           src_list=c.src_list)
+    J, g = ev.misfit_and_gradient(m)
+    assert J == Jr and torch.equal(g, gr)
 
 
 def test_device_invert_keeps_tensors_on_the_device():
