@@ -491,6 +491,9 @@ def main():
     # replicas: rank r owns the batch of shots r*C .. r*C+C-1
     shots = [(C * rank + i) % prob.n_shots for i in range(C)]
     tx, rx = element_csr(prob.geom, prob.shape, shots, None)
+    if not ckpt:   # the public API's default interval (one segment when it fits)
+        ckpt = backend.default_ckpt_k(prob.shape, prob.nt, rx.rows, len(rx.cell), C,
+                                      _lib.MODE_BORN if mode == "gn" else _lib.MODE_GRADIENT)
     plan = backend.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx, rx, batch=C, ckpt_k=ckpt)
     bmode = _lib.MODE_BORN if mode == "gn" else _lib.MODE_GRADIENT
     lib = _lib.load()
@@ -555,12 +558,16 @@ def main():
     value = C * world / (t_ms / 1000.0)
     cells = int(np.prod(prob.shape))
     hbm, peak_kind = _peaks()
+    one_seg = plan.info("nseg") == 1   # the forward writes every stash level: no recompute
     if mode == "gn":
-        pipeline_bytes = (56 * C + 24) * cells * (prob.nt - 1)
-        pipeline_model = "56 B/shot + 24 B/batch per cell-step (Born + checkpointed adjoint)"
+        a, b = (44, 28) if one_seg else (56, 24)
+        pipeline_model = (f"{a} B/shot + {b} B/batch per cell-step (Born + "
+                          + ("one-segment adjoint)" if one_seg else "checkpointed adjoint)"))
     else:
-        pipeline_bytes = (44 * C + 20) * cells * (prob.nt - 1)
-        pipeline_model = "44 B/shot + 20 B/batch per cell-step"
+        a, b = (32, 24) if one_seg else (44, 20)
+        pipeline_model = (f"{a} B/shot + {b} B/batch per cell-step"
+                          + (" (one checkpoint segment: no recompute)" if one_seg else ""))
+    pipeline_bytes = (a * C + b) * cells * (prob.nt - 1)
 
     # dominant kernel: the forward stencil launch, timed live (forward-only sweep)
     fws = bws

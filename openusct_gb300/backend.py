@@ -200,6 +200,29 @@ def batch_bytes_estimate(shape, nt, n_rx, nslot, C, ckpt_k, mode):
     return b
 
 
+def _available_bytes():
+    """(bytes the allocator can still hand out, device total): the driver's
+    free memory plus the blocks torch has cached but not in use."""
+    free, total = torch.cuda.mem_get_info()
+    return free + torch.cuda.memory_reserved() - torch.cuda.memory_allocated(), total
+
+
+def default_ckpt_k(shape, nt, n_rx, nslot, C, mode, avail=None, total=None):
+    """The checkpoint interval when the caller gives none.  One segment
+    (k = nt - 1: the forward sweep writes the d2p stash of every level and the
+    backward sweep recomputes nothing -- 12 C + 4 of the 44 C + 20 bytes per
+    cell-step saved) when that workspace fits in an eighth of the device and
+    half of what is available, as for 2D acquisitions; else 0, the engine's
+    memory-saving k = sqrt(2 (nt - 1)).  The gradient is bit-identical either
+    way."""
+    if mode < _lib.MODE_GRADIENT or int(nt) < 3:
+        return 0
+    if avail is None or total is None:
+        avail, total = _available_bytes()
+    need = batch_bytes_estimate(shape, nt, n_rx, nslot, C, int(nt) - 1, mode)
+    return int(nt) - 1 if need <= min(total // 8, avail // 2) else 0
+
+
 def choose_batch(shape, nt, n_tx, n_rx, nslot, ckpt_k, mode, budget):
     """Widest power-of-two shot batch (<= 64) whose workspace fits ``budget``."""
     C = 1
@@ -248,6 +271,8 @@ def _setup(m, geom, h, dt, nt, src_list, footprints, mode, batch, ckpt_k, tile):
         budget = int(0.7 * free)
         batch = choose_batch(shape, nt, tx.rows, rx.rows, len(rx.cell), ckpt_k or 0, mode,
                              budget)
+    if not ckpt_k and mode >= _lib.MODE_GRADIENT:
+        ckpt_k = default_ckpt_k(shape, nt, rx.rows, len(rx.cell), batch, mode)
     tile = tuple(tile) if tile else ()
     if len(tile) < 3:
         from .autotune import lookup
