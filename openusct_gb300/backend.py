@@ -122,13 +122,17 @@ class Plan:
 
     def workspace(self, kind, nbytes, device):
         """A workspace kept with the plan (stable buffers let captured graphs
-        replay); very large ones are not kept."""
+        replay).  One larger than an eighth of the device, or one that would
+        take the workspaces all cached plans hold past a quarter of it, is not
+        kept: memory a plan does not hold goes back to torch's allocator for
+        the caller's own tensors."""
         t = self._ws.get(kind)
         if t is not None and t.numel() >= nbytes:
             return t
         t = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
         total = torch.cuda.get_device_properties(device).total_memory
-        if nbytes <= total // 8:
+        if nbytes <= total // 8 and \
+                _held_workspace_bytes(self, kind) + nbytes <= total // WS_HOLD_DIV:
             self._ws[kind] = t
         return t
 
@@ -231,6 +235,25 @@ def choose_batch(shape, nt, n_tx, n_rx, nslot, ckpt_k, mode, budget):
     while C > 1 and batch_bytes_estimate(shape, nt, n_rx, nslot, C, ckpt_k, mode) > budget:
         C //= 2
     return C
+
+
+# cached plans together hold at most total memory // WS_HOLD_DIV of workspaces
+WS_HOLD_DIV = 4
+
+
+def _held_workspace_bytes(plan=None, kind=None):
+    """Bytes of the workspaces the cached plans hold, not counting ``plan``'s
+    workspace of ``kind`` (the one a new allocation replaces)."""
+    with _PLANS_LOCK:
+        plans = list(_PLANS.values())
+    if plan is not None and plan not in plans:
+        plans.append(plan)
+    held = 0
+    for p in plans:
+        for k, t in list(p._ws.items()):   # a copy made under the GIL
+            if not (p is plan and k == kind):
+                held += t.numel()
+    return held
 
 
 _PLANS: "OrderedDict[tuple, Plan]" = OrderedDict()

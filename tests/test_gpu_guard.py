@@ -139,3 +139,27 @@ def test_uploads_cast_on_the_device_equal_numpy_casts():
     for t in ts:
         t.join()
     assert not errs
+
+
+def test_cached_plans_hold_at_most_their_share_of_memory(monkeypatch):
+    """Workspaces kept with cached plans are capped in total: past the cap a
+    call still runs (its workspace is allocated for the call) and gives the
+    same result, and the held bytes stay under the cap."""
+    from openusct_gb300 import backend as gb
+    c = load("ring2d_point")
+    a = c.args()
+    gb.release()
+    total = torch.cuda.get_device_properties(0).total_memory
+    res = {}
+    for cap_div in (4, total):   # the default cap, then one that keeps nothing
+        monkeypatch.setattr(gb, "WS_HOLD_DIV", cap_div)
+        gb.release()
+        for shots in ([0], [1], [0, 1]):
+            J, g = gb.misfit_and_gradient(c["m0"], c.geom, a["wavelet"], c.dt, c.h, c.nt,
+                                          c["dobs"][shots], src_list=shots)
+            res.setdefault(tuple(shots), []).append((J, g))
+            assert gb._held_workspace_bytes() <= total // cap_div
+    for runs in res.values():
+        (J0, g0), (J1, g1) = runs
+        assert J0 == J1 and np.array_equal(g0, g1)
+    gb.release()
