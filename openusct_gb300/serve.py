@@ -128,7 +128,7 @@ class GpuExecutor:
         self.graphs = graphs
 
     def plan_for(self, req):
-        from .backend import Plan, choose_batch
+        from .backend import Plan, choose_batch, default_ckpt_k
         from .geometry import element_csr
         shape = tuple(req.m.shape)
         tx, rx = element_csr(req.geom, shape, req.src_list, req.footprints)
@@ -136,7 +136,10 @@ class GpuExecutor:
         C = req.batch or choose_batch(shape, req.nt, tx.rows, rx.rows, len(rx.cell), 0, mode,
                                       1 << 62)
         C = min(C, 32)
-        plan = Plan(shape, req.h, req.dt, req.nt, tx, rx, batch=C)
+        # the backend's default interval (one segment when its stash fits);
+        # the footprint used for admission is this plan's workspace
+        k = default_ckpt_k(shape, req.nt, rx.rows, len(rx.cell), C, mode)
+        plan = Plan(shape, req.h, req.dt, req.nt, tx, rx, batch=C, ckpt_k=k)
         if not self.graphs:
             plan.set("graphs", 0)
         return plan
