@@ -22,7 +22,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .backend import Plan, _on_exec_stream, _ptr, _stream, choose_batch
+from .backend import Plan, _on_exec_stream, _ptr, _stream, choose_batch, default_ckpt_k
 from .geometry import element_csr
 
 
@@ -39,6 +39,9 @@ class FMCProblem:
         if not batch:
             batch = choose_batch(self.shape, nt, tx.rows, rx.rows, len(rx.cell), ckpt_k or 0,
                                  _lib.MODE_GRADIENT, int(0.4 * free))
+        if not ckpt_k:   # the backend's default (one segment when its stash fits)
+            ckpt_k = default_ckpt_k(self.shape, nt, rx.rows, len(rx.cell), batch,
+                                    _lib.MODE_GRADIENT)
         self.plan = Plan(self.shape, h, dt, nt, tx, rx, batch=batch, ckpt_k=ckpt_k or 0)
         from .backend import _grid_array, _wavelet
         self.wavelet = _wavelet(wavelet, nt, self.device)
