@@ -42,7 +42,9 @@ os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
 
 METRIC = "Grad shots/s + p50/p99, batched serve vs per-shot plain, same GB300, relerr≤1e-4"
 WORKLOAD = ("3D acoustic cylinder FMC L2 gradient, 192^3, dx=0.2mm, 8x32 elements (256 shots), "
-            "nt=2000, FP32, 32 shots per launch, checkpoint every 64 steps")
+            "nt=2000, FP32, 32 shots per launch, checkpoint segments sized to HBM (the last, "
+            "never recomputed, as long as 70% of the device allows)")
+TAIL = -1   # k0 sentinel: the interval with the longest unrecomputed last segment that fits
 
 # name -> (description, problem builder, shots per launch, checkpoint k, mode)
 #   mode "grad": one step = the L2 gradient of one batch (model: 44 B/shot + 20 B/batch
@@ -50,18 +52,49 @@ WORKLOAD = ("3D acoustic cylinder FMC L2 gradient, 192^3, dx=0.2mm, 8x32 element
 #   (44 + 12 B/shot + 24 B/batch)
 WORKLOADS = {
     "grad3d": (WORKLOAD, lambda: __import__("openusct_gb300.problems").problems.cylinder3d(seed=0),
-               32, 64, "grad"),
+               32, TAIL, "grad"),
     "ring2d": ("2D ring FWI L2 gradient, 256^2, dx=0.15mm, 64-element ring r=16mm, two seeded "
                "discs, 1 MHz Ricker, nt=1500, FP32, all 64 shots in one launch",
                lambda: __import__("openusct_gb300.problems").problems.ring2d(seed=0), 64, 0, "grad"),
     "gn3d": ("3D Gauss-Newton Hessian-vector product (Born + adjoint), 224^3, dx=0.18mm, 8x32 "
              "elements (256 shots), nt=2500, FP32, 16 shots per launch",
-             lambda: __import__("openusct_gb300.problems").problems.gn3d(seed=0), 16, 0, "gn"),
+             lambda: __import__("openusct_gb300.problems").problems.gn3d(seed=0), 16, TAIL, "gn"),
     "grad3d_large": ("3D cylinder FMC L2 gradient, 320^3, dx=0.12mm, 16x32 elements (512 shots), "
                      "nt=3000, FP32, 8 shots per launch",
                      lambda: __import__("openusct_gb300.problems").problems.cylinder3d_large(seed=0),
-                     8, 0, "grad"),
+                     8, TAIL, "grad"),
 }
+
+
+def tail_ckpt_k(shape, nt, n_rx, nslot, C, mode, budget_bytes):
+    """The checkpoint interval whose last segment -- the levels the forward
+    sweep stashes itself, so the backward never recomputes them -- is longest
+    while the batch workspace fits ``budget_bytes`` (ties: less memory)."""
+    from openusct_gb300.backend import batch_bytes_estimate
+    best = (0, 0, 2)
+    for k in range(2, nt):
+        need = batch_bytes_estimate(shape, nt, n_rx, nslot, C, k, mode)
+        if need > budget_bytes:
+            continue
+        nseg = (nt - 1 + k - 1) // k
+        tail = nt - 1 - (nseg - 1) * k
+        if (tail, -need) > best[:2]:
+            best = (tail, -need, k)
+    return best[2]
+
+
+def schedule_bytes(cells, C, nt, k, mode):
+    """Algorithmic bytes of one batch through the engine's schedule: the
+    forward sweep (12 C + 4, Born 24 C + 8 per cell-step) on every level, the
+    d2p stash it writes on the last segment's levels (4 C), the segment
+    recompute (16 C + 4) on every other level, the adjoint (16 C + 20: S and
+    the FP64 gradient read-modify-write per batch) on every level."""
+    k = min(max(2, k), max(2, nt - 1))
+    nseg = (nt - 1 + k - 1) // k
+    rec = (nseg - 1) * k
+    tail = nt - 1 - rec
+    fwd = 24 * C + 8 if mode == "gn" else 12 * C + 4
+    return cells * ((nt - 1) * (fwd + 16 * C + 20) + tail * 4 * C + rec * (16 * C + 4)), rec, tail
 
 
 def _peaks():
@@ -491,9 +524,14 @@ def main():
     # replicas: rank r owns the batch of shots r*C .. r*C+C-1
     shots = [(C * rank + i) % prob.n_shots for i in range(C)]
     tx, rx = element_csr(prob.geom, prob.shape, shots, None)
-    if not ckpt:   # the public API's default interval (one segment when it fits)
-        ckpt = backend.default_ckpt_k(prob.shape, prob.nt, rx.rows, len(rx.cell), C,
-                                      _lib.MODE_BORN if mode == "gn" else _lib.MODE_GRADIENT)
+    bmode_ = _lib.MODE_BORN if mode == "gn" else _lib.MODE_GRADIENT
+    if ckpt == TAIL:
+        import torch
+        total = torch.cuda.get_device_properties(0).total_memory
+        ckpt = tail_ckpt_k(prob.shape, prob.nt, rx.rows, len(rx.cell), C, bmode_,
+                           int(0.7 * total))
+    elif not ckpt:   # the public API's default interval (one segment when it fits)
+        ckpt = backend.default_ckpt_k(prob.shape, prob.nt, rx.rows, len(rx.cell), C, bmode_)
     plan = backend.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx, rx, batch=C, ckpt_k=ckpt)
     bmode = _lib.MODE_BORN if mode == "gn" else _lib.MODE_GRADIENT
     lib = _lib.load()
@@ -558,16 +596,11 @@ def main():
     value = C * world / (t_ms / 1000.0)
     cells = int(np.prod(prob.shape))
     hbm, peak_kind = _peaks()
-    one_seg = plan.info("nseg") == 1   # the forward writes every stash level: no recompute
-    if mode == "gn":
-        a, b = (44, 28) if one_seg else (56, 24)
-        pipeline_model = (f"{a} B/shot + {b} B/batch per cell-step (Born + "
-                          + ("one-segment adjoint)" if one_seg else "checkpointed adjoint)"))
-    else:
-        a, b = (32, 24) if one_seg else (44, 20)
-        pipeline_model = (f"{a} B/shot + {b} B/batch per cell-step"
-                          + (" (one checkpoint segment: no recompute)" if one_seg else ""))
-    pipeline_bytes = (a * C + b) * cells * (prob.nt - 1)
+    pipeline_bytes, rec_lv, tail_lv = schedule_bytes(cells, C, prob.nt, plan.info("ckpt_k"), mode)
+    pipeline_model = (("Born forward 24C+8" if mode == "gn" else "forward 12C+4")
+                      + f" and adjoint 16C+20 B per cell on all {prob.nt - 1} levels, stash 4C on "
+                      f"the {tail_lv} levels of the last segment, recompute 16C+4 on the other "
+                      f"{rec_lv} (k = {plan.info('ckpt_k')})")
 
     # dominant kernel: the forward stencil launch, timed live (forward-only sweep)
     fws = bws
