@@ -18,7 +18,6 @@ and the backward re-runs each batch's forward sweep before reversing it.
 
 from __future__ import annotations
 
-import numpy as np
 import torch
 
 from . import _lib
