@@ -275,3 +275,35 @@ def test_make_sponge_matches_the_reference_and_extends_to_3d():
             sys.path.remove(ref)
         for shape, w, s in (((64, 80), 10, 0.1), ((101, 101), 25, 0.08), ((50, 200), 20, 0.05)):
             assert np.array_equal(make_sponge(shape, w, s), ref_sponge(shape, w, s))
+
+
+def test_bench_schedule_bytes_and_tail_interval():
+    """The pipeline byte count bench.py reports: forward and adjoint on every
+    level, the stash on the last segment, the recompute on the others; one
+    segment is 32 C + 24 B per cell-step.  The HBM-sized interval maximises
+    the never-recomputed last segment within the budget."""
+    import importlib.util
+    import os
+    from openusct_gb300 import _lib
+    from openusct_gb300.backend import batch_bytes_estimate
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    cells, C, nt = 1000, 32, 2000
+    one, rec, tail = bench.schedule_bytes(cells, C, nt, nt - 1, "grad")
+    assert (rec, tail) == (0, nt - 1) and one == cells * (nt - 1) * (32 * C + 24)
+    b64, rec, tail = bench.schedule_bytes(cells, C, nt, 64, "grad")
+    assert (rec, tail) == (31 * 64, 1999 - 31 * 64)
+    assert b64 == cells * (1999 * (12 * C + 4 + 16 * C + 20) + tail * 4 * C + rec * (16 * C + 4))
+    gn, _, _ = bench.schedule_bytes(cells, C, nt, 64, "gn")
+    assert gn - b64 == cells * 1999 * (12 * C + 4)
+    shape, n_rx = (192, 192, 192), 256
+    budget = int(0.7 * 284208 * 2 ** 20)
+    k = bench.tail_ckpt_k(shape, nt, n_rx, n_rx, C, _lib.MODE_GRADIENT, budget)
+    assert batch_bytes_estimate(shape, nt, n_rx, n_rx, C, k, _lib.MODE_GRADIENT) <= budget
+    _, _, tail_k = bench.schedule_bytes(1, C, nt, k, "grad")
+    for kk in range(2, nt):
+        if batch_bytes_estimate(shape, nt, n_rx, n_rx, C, kk, _lib.MODE_GRADIENT) <= budget:
+            assert bench.schedule_bytes(1, C, nt, kk, "grad")[2] <= tail_k
+    assert k == 200 and tail_k == 199
