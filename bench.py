@@ -42,45 +42,28 @@ os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
 
 METRIC = "Grad shots/s + p50/p99, batched serve vs per-shot plain, same GB300, relerr≤1e-4"
 WORKLOAD = ("3D acoustic cylinder FMC L2 gradient, 192^3, dx=0.2mm, 8x32 elements (256 shots), "
-            "nt=2000, FP32, 32 shots per launch, checkpoint segments sized to HBM (the last, "
-            "never recomputed, as long as 70% of the device allows)")
-TAIL = -1   # k0 sentinel: the interval with the longest unrecomputed last segment that fits
+            "nt=2000, FP32, 32 shots per launch, the backend's default checkpoint interval (the "
+            "last segment, never recomputed, as long as 70% of the device allows)")
 
-# name -> (description, problem builder, shots per launch, checkpoint k, mode)
+# name -> (description, problem builder, shots per launch, checkpoint k (0: the
+# backend's default interval), mode)
 #   mode "grad": one step = the L2 gradient of one batch (model: 44 B/shot + 20 B/batch
 #   per cell-step); "gn": one step = the Gauss-Newton product of one batch
 #   (44 + 12 B/shot + 24 B/batch)
 WORKLOADS = {
     "grad3d": (WORKLOAD, lambda: __import__("openusct_gb300.problems").problems.cylinder3d(seed=0),
-               32, TAIL, "grad"),
+               32, 0, "grad"),
     "ring2d": ("2D ring FWI L2 gradient, 256^2, dx=0.15mm, 64-element ring r=16mm, two seeded "
                "discs, 1 MHz Ricker, nt=1500, FP32, all 64 shots in one launch",
                lambda: __import__("openusct_gb300.problems").problems.ring2d(seed=0), 64, 0, "grad"),
     "gn3d": ("3D Gauss-Newton Hessian-vector product (Born + adjoint), 224^3, dx=0.18mm, 8x32 "
              "elements (256 shots), nt=2500, FP32, 16 shots per launch",
-             lambda: __import__("openusct_gb300.problems").problems.gn3d(seed=0), 16, TAIL, "gn"),
+             lambda: __import__("openusct_gb300.problems").problems.gn3d(seed=0), 16, 0, "gn"),
     "grad3d_large": ("3D cylinder FMC L2 gradient, 320^3, dx=0.12mm, 16x32 elements (512 shots), "
                      "nt=3000, FP32, 8 shots per launch",
                      lambda: __import__("openusct_gb300.problems").problems.cylinder3d_large(seed=0),
-                     8, TAIL, "grad"),
+                     8, 0, "grad"),
 }
-
-
-def tail_ckpt_k(shape, nt, n_rx, nslot, C, mode, budget_bytes):
-    """The checkpoint interval whose last segment -- the levels the forward
-    sweep stashes itself, so the backward never recomputes them -- is longest
-    while the batch workspace fits ``budget_bytes`` (ties: less memory)."""
-    from openusct_gb300.backend import batch_bytes_estimate
-    best = (0, 0, 2)
-    for k in range(2, nt):
-        need = batch_bytes_estimate(shape, nt, n_rx, nslot, C, k, mode)
-        if need > budget_bytes:
-            continue
-        nseg = (nt - 1 + k - 1) // k
-        tail = nt - 1 - (nseg - 1) * k
-        if (tail, -need) > best[:2]:
-            best = (tail, -need, k)
-    return best[2]
 
 
 def schedule_bytes(cells, C, nt, k, mode):
@@ -155,31 +138,61 @@ class Clocks:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_gradient_sample(prob, shot, nt_sample, k, mode="grad", misfit="l2"):
-    """Time the FP64 oracle gradient (or Gauss-Newton product) for one shot over
-    nt_sample levels and scale to the full time axis: (shots/s, seconds, text)."""
+def host_available_bytes():
+    """MemAvailable of this host (bytes), 0 when it cannot be read."""
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def cpu_shot_interval(prob, mode, frac=0.5):
+    """The FP64 oracle's memory plan for one whole shot on this host: k = 0 --
+    the full history of every level, no recompute, the reference core's own
+    plan (libuap.hpp:179-186) -- when that history fits ``frac`` of the
+    available host memory, else the longest checkpoint interval whose
+    checkpoints and segment fit (the Gauss-Newton restatement always
+    checkpoints).  Returns (k, bytes)."""
+    import numpy as np
+    N = int(np.prod(prob.shape))
+    nt = prob.nt
+    avail = host_available_bytes() or (64 << 30)
+    budget = frac * avail
+    hist = nt * N * 8
+    if mode != "gn" and hist <= budget:
+        return 0, hist
+    for k in range(nt - 1, 1, -1):
+        nseg = (nt - 1 + k - 1) // k
+        need = (2 * nseg + k + 2 + (4 if mode == "gn" else 0)) * N * 8
+        if need <= budget:
+            return k, need
+    return 2, (2 * (nt - 1) + 8) * N * 8
+
+
+def cpu_whole_shot(prob, shot, k, dobs1=None, mode="grad", misfit="l2"):
+    """Time the FP64 oracle's gradient (or Gauss-Newton product) of one whole
+    shot over the full time axis with memory plan k: (seconds, text)."""
     import numpy as np
     import oracle
-    nt_sample = min(nt_sample, prob.nt)
-    wav = prob.wavelet[:nt_sample]
     geom = prob.geom
     if mode == "gn":
         t0 = time.perf_counter()
-        oracle.gn_hessian_vector(prob.m0, geom, wav, prob.dt, prob.h, nt_sample, prob.v,
+        oracle.gn_hessian_vector(prob.m0, geom, prob.wavelet, prob.dt, prob.h, prob.nt, prob.v,
                                  src_list=[shot], k=k)
-        dt_s = time.perf_counter() - t0
-        per_shot = dt_s * (prob.nt - 1) / (nt_sample - 1)
-        return 1.0 / per_shot, dt_s, (f"1 shot x {nt_sample} levels of the Gauss-Newton product "
-                                      f"(checkpoint k={k}), scaled by (nt-1)/{nt_sample - 1}")
-    rec_all = oracle.forward_fmc(prob.m_true, geom, wav, prob.dt, prob.h, nt_sample, None, [shot])
+        return time.perf_counter() - t0, (f"1 whole shot ({prob.nt} levels) of the Gauss-Newton "
+                                          f"product, background checkpointed every {k} steps")
     t0 = time.perf_counter()
-    oracle.misfit_and_gradient(prob.m0, geom, wav, prob.dt, prob.h, nt_sample, rec_all, None,
-                               [shot], k=k, misfit_type=misfit)
-    dt_s = time.perf_counter() - t0
-    per_shot = dt_s * (prob.nt - 1) / (nt_sample - 1)
+    oracle.misfit_and_gradient(prob.m0, geom, prob.wavelet, prob.dt, prob.h, prob.nt,
+                               np.asarray(dobs1, np.float64), None, [shot], k=k,
+                               misfit_type=misfit)
     grid = "x".join(str(v) for v in prob.shape)
-    return 1.0 / per_shot, dt_s, (f"1 shot x {nt_sample} levels of the {grid} gradient "
-                                  f"(checkpoint k={k}), scaled by (nt-1)/{nt_sample - 1}")
+    plan = ("full history, no recompute (the reference core's memory plan)" if k == 0 else
+            f"checkpoints every {k} steps (the full history does not fit this host)")
+    return time.perf_counter() - t0, f"1 whole shot ({prob.nt} levels) of the {grid} gradient, {plan}"
 
 
 SERVE_STREAM = ("seeded Poisson stream at 20 req/s, 30% gradient / 70% forward, half 2D rings "
@@ -236,26 +249,38 @@ def serve_phase(args):
 
 
 def run_reference(args, prob, desc_w, mode):
-    """--impl reference: the reference scheme's CPU path on the host cores."""
+    """--impl reference: the reference scheme's CPU path on the host cores.
+    One step = the gradient (or Gauss-Newton product) of one whole shot over
+    the full time axis, by the oracle's FP64 restatement of the reference core
+    (bit-identical to it), with the reference's full-history memory plan when
+    it fits this host.  The observed data of the shot come from one untimed
+    FP64 forward run."""
     import oracle
     oracle.build()
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     kind = "port"
-    nt_sample = 24 if len(prob.shape) == 3 else 300
-    vals = []
+    k, mem = cpu_shot_interval(prob, mode)
+    shot = 0
+    dobs1 = None
+    if mode != "gn":
+        dobs1 = oracle.forward_fmc(prob.m_true, prob.geom, prob.wavelet, prob.dt, prob.h,
+                                   prob.nt, None, [shot])
+    secs = []
+    desc = ""
     for i in range(args.warmup + args.steps):
-        v, secs, desc = cpu_gradient_sample(prob, i % prob.n_shots, nt_sample, 8, mode)
+        s_i, desc = cpu_whole_shot(prob, shot, k, dobs1, mode)
         if i >= args.warmup:
-            vals.append((v, secs))
-    value = statistics.median(v for v, _ in vals)
-    ms = 1000.0 / value
+            secs.append(s_i)
+    ms = 1000.0 * sum(secs) / len(secs)
+    value = 1000.0 / ms
     line = {"metric": METRIC, "value": value, "unit": "shots/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
             "config": {"workload": desc_w, "l2": "inputs larger than L2"},
             "cpu_baseline": {"value": value, "unit": "shots/s", "cores": cores, "kind": kind,
-                             "sample": desc},
+                             "sample": desc, "host_bytes": mem,
+                             "seconds_per_step": [round(v, 3) for v in secs]},
             "e2e": {"value": value, "unit": "shots/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -525,12 +550,7 @@ def main():
     shots = [(C * rank + i) % prob.n_shots for i in range(C)]
     tx, rx = element_csr(prob.geom, prob.shape, shots, None)
     bmode_ = _lib.MODE_BORN if mode == "gn" else _lib.MODE_GRADIENT
-    if ckpt == TAIL:
-        import torch
-        total = torch.cuda.get_device_properties(0).total_memory
-        ckpt = tail_ckpt_k(prob.shape, prob.nt, rx.rows, len(rx.cell), C, bmode_,
-                           int(0.7 * total))
-    elif not ckpt:   # the public API's default interval (one segment when it fits)
+    if not ckpt:   # the public API's default interval (the same the e2e call below gets)
         ckpt = backend.default_ckpt_k(prob.shape, prob.nt, rx.rows, len(rx.cell), C, bmode_)
     plan = backend.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx, rx, batch=C, ckpt_k=ckpt)
     bmode = _lib.MODE_BORN if mode == "gn" else _lib.MODE_GRADIENT
@@ -640,7 +660,8 @@ def main():
     # between barriers; the job's rate uses the slowest rank
     m0_h = prob.m0
     dobs_h = dobs.double().cpu().numpy()
-    kw = dict(src_list=shots, batch=C, ckpt_k=ckpt or None)
+    # the public API's own checkpoint interval unless --ckpt names one
+    kw = dict(src_list=shots, batch=C, ckpt_k=args.ckpt if args.ckpt > 0 else None)
     tw_h = tw.cpu().numpy() if tw is not None else None
     call = (lambda: backend.gn_hessian_vector(m0_h, prob.geom, prob.wavelet, prob.dt, prob.h,
                                               prob.nt, prob.v, **kw)) if mode == "gn" else \
@@ -691,12 +712,16 @@ def main():
         args_p = (pplan.handle, P(m0), P(wav), P(d1), P(J1), P(g), P(pws), sp)
         _lib.check(lib.usct_plain_misfit_and_gradient_dev(*args_p))
         torch.cuda.synchronize()
-        e0.record(s)
-        _lib.check(lib.usct_plain_misfit_and_gradient_dev(*args_p))
-        e1.record(s)
-        torch.cuda.synchronize()
-        tp = e0.elapsed_time(e1) / 1000.0
+        times = []
+        for _ in range(3):   # the median of three timed calls
+            e0.record(s)
+            _lib.check(lib.usct_plain_misfit_and_gradient_dev(*args_p))
+            e1.record(s)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1000.0)
+        tp = statistics.median(times)
         plain = {"value": 1.0 / tp, "unit": "shots/s", "ms_per_shot": tp * 1000.0,
+                 "ms_per_shot_runs": [t * 1000.0 for t in times],
                  "speedup_batched_vs_plain": value / world / (1.0 / tp)}
         del pws
 
@@ -712,13 +737,16 @@ def main():
         try:
             import oracle
             oracle.build()
-            v, secs, desc = cpu_gradient_sample(prob, 0, 40 if len(prob.shape) == 3 else 600, 8,
-                                                mode, args.misfit)
+            # the same procedure as the reference arm: one whole shot, timed
+            kc, mem = cpu_shot_interval(prob, mode)
+            d1 = dobs[0:1].double().cpu().numpy() if mode != "gn" else None
+            secs, desc = cpu_whole_shot(prob, shots[0], kc, d1, mode, args.misfit)
+            v = 1.0 / secs
             if tw is not None:
                 desc += "; without the data windows (an elementwise product of the residual)"
             cpu = {"value": v, "unit": "shots/s",
                    "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
-                   "kind": "port", "sample": desc, "seconds": secs}
+                   "kind": "port", "sample": desc, "seconds": secs, "host_bytes": mem}
         except Exception as exc:  # the baseline is reported, never required
             cpu = {"value": None, "error": str(exc)[:200]}
 

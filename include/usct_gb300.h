@@ -272,8 +272,13 @@ int usct_misfit_and_gradient_mt(const double* m, const int* dims, int ndim, doub
  *   m, sponge (NULL = none), wavelet: device FP64; data: device FP32
  *   [n_tx][nt][n_rx], caller-allocated.
  * The first call on a device resolves the array's device address (with that
- * device current); make it before any stream capture.  Calls share the array:
- * calls that overlap on the GPU race on it and must be serialised.
+ * device current); make it before any stream capture.  The address is kept per
+ * device and context, and resolved again when another context is current.
+ * Each call uploads per-tile source/receiver lists from host memory local to
+ * the call, so a call on a capturing stream returns USCT_ERR_ARG before it
+ * enqueues anything.  NULL tx_cell/tx_w (with sources) or rx_cell/rx_w give
+ * USCT_ERR_ARG.  Calls share the array: calls that overlap on the GPU race on
+ * it and must be serialised.
  */
 #define USCT_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 int usct_forward_fmc_noalloc(int ndim, const int* dims, double h, double dt, int nt,

@@ -21,7 +21,8 @@ from __future__ import annotations
 import torch
 
 from . import _lib
-from .backend import Plan, _on_exec_stream, _ptr, _stream, choose_batch, default_ckpt_k
+from .backend import (Plan, _on_exec_stream, _ptr, _stream, batch_bytes_estimate, choose_batch,
+                      default_ckpt_k)
 from .geometry import element_csr
 
 
@@ -38,14 +39,21 @@ class FMCProblem:
         if not batch:
             batch = choose_batch(self.shape, nt, tx.rows, rx.rows, len(rx.cell), ckpt_k or 0,
                                  _lib.MODE_GRADIENT, int(0.4 * free))
-        if not ckpt_k:   # the backend's default (one segment when its stash fits)
+        keep = int(0.5 * free) if keep_bytes is None else int(keep_bytes)
+        if not ckpt_k:
+            # the backend's default interval; when every batch's checkpoints can
+            # be kept from forward to backward, sized so that they all fit
+            nb = -(-tx.rows // batch)
+            least = batch_bytes_estimate(self.shape, nt, rx.rows, len(rx.cell), batch, 0,
+                                         _lib.MODE_GRADIENT)
+            share = keep // nb if keep // nb >= least else None
             ckpt_k = default_ckpt_k(self.shape, nt, rx.rows, len(rx.cell), batch,
-                                    _lib.MODE_GRADIENT)
+                                    _lib.MODE_GRADIENT, budget_bytes=share)
         self.plan = Plan(self.shape, h, dt, nt, tx, rx, batch=batch, ckpt_k=ckpt_k or 0)
         from .backend import _grid_array, _wavelet
         self.wavelet = _wavelet(wavelet, nt, self.device)
         self.sponge = _grid_array(sponge, shape, "sponge", self.device)
-        self.keep_bytes = int(0.5 * free) if keep_bytes is None else int(keep_bytes)
+        self.keep_bytes = keep
         self.n_tx, self.nt, self.n_rx = self.plan.n_tx, self.plan.nt, self.plan.n_rx
 
 

@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import ctypes
 import threading
+import weakref
 from collections import OrderedDict
 
 import numpy as np
@@ -115,6 +116,8 @@ class Plan:
             self.set("stages", int(stages))
         self._ws = {}
         self.lock = threading.RLock()
+        with _PLANS_LOCK:
+            _LIVE_PLANS.add(self)
         # launch-bound sizes replay whole batch sweeps as CUDA graphs
         level = int(np.prod(self.shape)) * max(1, self.batch)
         if level <= (1 << 22):
@@ -211,20 +214,74 @@ def _available_bytes():
     return free + torch.cuda.memory_reserved() - torch.cuda.memory_allocated(), total
 
 
-def default_ckpt_k(shape, nt, n_rx, nslot, C, mode, avail=None, total=None):
-    """The checkpoint interval when the caller gives none.  One segment
-    (k = nt - 1: the forward sweep writes the d2p stash of every level and the
-    backward sweep recomputes nothing -- 12 C + 4 of the 44 C + 20 bytes per
-    cell-step saved) when that workspace fits in an eighth of the device and
-    half of what is available, as for 2D acquisitions; else 0, the engine's
-    memory-saving k = sqrt(2 (nt - 1)).  The gradient is bit-identical either
-    way."""
+# Share of the device one gradient workspace may take when the caller gives no
+# checkpoint interval; set_workspace_fraction lowers (or raises) it.
+_WORKSPACE_FRACTION = 0.7
+_DEFAULT_K = {}
+_DEFAULT_K_LOCK = threading.Lock()
+
+
+def set_workspace_fraction(fraction):
+    """Cap, as a share of the device's memory, the batch workspace a gradient
+    or Gauss-Newton call sizes for itself when it is given no checkpoint
+    interval (default 0.7).  Intervals already chosen are forgotten."""
+    global _WORKSPACE_FRACTION
+    f = float(fraction)
+    if not 0.0 < f <= 0.95:
+        raise ValueError(f"workspace fraction must be in (0, 0.95], got {fraction}")
+    with _DEFAULT_K_LOCK:
+        _WORKSPACE_FRACTION = f
+        _DEFAULT_K.clear()
+
+
+def tail_ckpt_k(shape, nt, n_rx, nslot, C, mode, budget_bytes):
+    """The checkpoint interval whose last segment -- the levels the forward
+    sweep stashes itself, so the backward sweep never recomputes them -- is the
+    longest while the batch workspace fits ``budget_bytes`` (ties: the smaller
+    workspace); k = nt - 1 (one segment, nothing recomputed) when everything
+    fits, 0 when not even the smallest workspace does."""
+    nt = int(nt)
+    best = None
+    for k in range(2, nt):
+        need = batch_bytes_estimate(shape, nt, n_rx, nslot, C, k, mode)
+        if need > budget_bytes:
+            continue
+        nseg = (nt - 1 + k - 1) // k
+        tail = nt - 1 - (nseg - 1) * k
+        if best is None or (tail, -need) > best[:2]:
+            best = (tail, -need, k)
+    return best[2] if best else 0
+
+
+def default_ckpt_k(shape, nt, n_rx, nslot, C, mode, avail=None, total=None, budget_bytes=None):
+    """The checkpoint interval when the caller gives none: the one whose last
+    segment (stashed by the forward sweep itself, never recomputed) is the
+    longest while the batch workspace fits ``budget_bytes`` -- by default the
+    workspace fraction (0.7) of the device, and never more than 90 % of what
+    is available.  One segment (k = nt - 1, nothing recomputed: 32 C + 24
+    instead of 44 C + 28 bytes per cell-step) when the whole stash fits, as for
+    2D acquisitions; at the 192^3 / 32-shot gradient k = 200 (a 203 GB
+    workspace: only the last 199 of 1999 levels are not recomputed).  0 (the
+    engine's memory-saving k = sqrt(2 (nt - 1))) when nothing fits.  The
+    gradient is bit-identical for every k.  The choice is made once per problem
+    and device and then kept, so plans do not change with memory pressure."""
     if mode < _lib.MODE_GRADIENT or int(nt) < 3:
         return 0
-    if avail is None or total is None:
+    dev = torch.cuda.current_device() if torch.cuda.is_available() else -1
+    key = (tuple(int(s) for s in shape), int(nt), int(n_rx), int(nslot), int(C), int(mode), dev,
+           None if budget_bytes is None else int(budget_bytes), _WORKSPACE_FRACTION)
+    measured = avail is None or total is None
+    if measured:
+        with _DEFAULT_K_LOCK:
+            if key in _DEFAULT_K:
+                return _DEFAULT_K[key]
         avail, total = _available_bytes()
-    need = batch_bytes_estimate(shape, nt, n_rx, nslot, C, int(nt) - 1, mode)
-    return int(nt) - 1 if need <= min(total // 8, avail // 2) else 0
+    cap = _WORKSPACE_FRACTION * total if budget_bytes is None else budget_bytes
+    k = tail_ckpt_k(shape, nt, n_rx, nslot, C, mode, int(min(cap, 0.9 * avail)))
+    if measured:   # only what the device itself said is remembered
+        with _DEFAULT_K_LOCK:
+            _DEFAULT_K[key] = k
+    return k
 
 
 def choose_batch(shape, nt, n_tx, n_rx, nslot, ckpt_k, mode, budget):
@@ -242,10 +299,11 @@ WS_HOLD_DIV = 4
 
 
 def _held_workspace_bytes(plan=None, kind=None):
-    """Bytes of the workspaces the cached plans hold, not counting ``plan``'s
+    """Bytes of the workspaces every live plan holds (cached ones, and ones
+    evicted from the cache that a caller still uses), not counting ``plan``'s
     workspace of ``kind`` (the one a new allocation replaces)."""
     with _PLANS_LOCK:
-        plans = list(_PLANS.values())
+        plans = list(_LIVE_PLANS)
     if plan is not None and plan not in plans:
         plans.append(plan)
     held = 0
@@ -257,6 +315,7 @@ def _held_workspace_bytes(plan=None, kind=None):
 
 
 _PLANS: "OrderedDict[tuple, Plan]" = OrderedDict()
+_LIVE_PLANS: "weakref.WeakSet[Plan]" = weakref.WeakSet()
 _MAX_PLANS = 8
 _PLANS_LOCK = threading.Lock()
 

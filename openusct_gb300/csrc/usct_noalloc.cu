@@ -19,15 +19,21 @@
 //
 // The array's name is not a device address in host code, so the first call on
 // each device resolves it once with cudaGetSymbolAddress (that device must be
-// current); make that first call before any stream capture.  All calls share
-// the array and it keeps the previous call's contents: each call clears the
-// wavefield levels and the level-0 receiver row it relies on being zero, and
-// calls that overlap on the GPU (two streams, two host threads) race on the
-// array -- serialise them.
+// current); make that first call before any stream capture.  The address is
+// kept per device together with the context it was resolved in, and resolved
+// again when another context is current on that device (after a
+// cudaDeviceReset, or a context the caller made current itself).  Every call
+// uploads its per-tile source and receiver lists from host memory local to the
+// call, so a call on a stream that is capturing is refused with USCT_ERR_ARG
+// before it enqueues anything.  All calls share the array and it keeps the
+// previous call's contents: each call clears the wavefield levels and the
+// level-0 receiver row it relies on being zero, and calls that overlap on the
+// GPU (two streams, two host threads) race on the array -- serialise them.
 //
 // The stencil is the same k_forward kernel as the batched engine, run one
 // transmit at a time (one shot channel), so the traces equal those of
 // usct_forward_fmc_dev.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -49,23 +55,48 @@ namespace {
 
 std::mutex g_scratch_mu;
 void* g_scratch_ptr[256] = {};
+CUcontext g_scratch_ctx[256] = {};
+
+// the driver's cuCtxGetCurrent, looked up once through the runtime (the
+// library links no driver library of its own)
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+CtxGetCurrentFn ctx_get_current() {
+    static CtxGetCurrentFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (CtxGetCurrentFn)f;
+    });
+    return fn;
+}
 
 int scratch_address(void** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return usct_internal_error(USCT_ERR_CUDA, cudaGetErrorString(e));
     if (dev < 0 || dev >= 256) return usct_internal_error(USCT_ERR_ARG, "device ordinal out of range");
+    CtxGetCurrentFn get = ctx_get_current();
+    if (!get) return usct_internal_error(USCT_ERR_CUDA, "cuCtxGetCurrent is not available");
+    CUcontext ctx = nullptr;
+    if (get(&ctx) != CUDA_SUCCESS) ctx = nullptr;   // none yet: the runtime makes one below
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (!ctx || !g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);   // makes the primary context current if needed
         if (e != cudaSuccess || !p) {
             char msg[256];
             snprintf(msg, sizeof(msg), "cudaGetSymbolAddress of the static scratch failed: %s",
                      cudaGetErrorString(e));
             return usct_internal_error(USCT_ERR_CUDA, msg);
         }
+        if (get(&ctx) != CUDA_SUCCESS || !ctx)
+            return usct_internal_error(USCT_ERR_CUDA, "no current CUDA context for the static scratch");
         g_scratch_ptr[dev] = p;
+        g_scratch_ctx[dev] = ctx;
     }
     *out = g_scratch_ptr[dev];
     return USCT_OK;
@@ -120,6 +151,10 @@ extern "C" int usct_forward_fmc_noalloc(int ndim, const int* dims, double h, dou
     if (ndim != 2 && ndim != 3) return usct_internal_error(USCT_ERR_ARG, "ndim must be 2 or 3");
     if (!dims || !tx_ptr || !rx_ptr || !m || !wavelet || !data)
         return usct_internal_error(USCT_ERR_ARG, "null argument");
+    if (n_tx >= 1 && tx_ptr[n_tx] > 0 && (!tx_cell || !tx_w))
+        return usct_internal_error(USCT_ERR_ARG, "null source cell or weight array");
+    if (n_rx >= 1 && (!rx_cell || !rx_w))
+        return usct_internal_error(USCT_ERR_ARG, "null receiver cell or weight array");
     for (int d = 0; d < ndim; ++d)
         if (dims[d] < 3) return usct_internal_error(USCT_ERR_ARG, "every grid extent must be >= 3");
     if (nt < 2 || n_tx < 1 || n_rx < 1 || !(h > 0) || !(dt > 0))
@@ -226,10 +261,20 @@ extern "C" int usct_forward_fmc_noalloc(int ndim, const int* dims, double h, dou
     }
 
     // ---- device side: carve the static scratch ----
+    cudaStream_t s = (cudaStream_t)stream;
+    {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        const cudaError_t e = cudaStreamIsCapturing(s, &cs);
+        if (e != cudaSuccess) return usct_internal_error(USCT_ERR_CUDA, cudaGetErrorString(e));
+        if (cs != cudaStreamCaptureStatusNone)
+            return usct_internal_error(USCT_ERR_ARG,
+                                       "usct_forward_fmc_noalloc: the stream is capturing; this "
+                                       "entry point uploads host lists local to the call and "
+                                       "cannot be captured");
+    }
     void* base = nullptr;
     int rc = scratch_address(&base);
     if (rc != USCT_OK) return rc;
-    cudaStream_t s = (cudaStream_t)stream;
     char* c = (char*)base;
     float* S = (float*)c; c += b_S;
     float* sp = sponge ? (float*)c : nullptr; c += b_sp;

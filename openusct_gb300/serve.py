@@ -121,11 +121,15 @@ def percentile(xs, q):
 class GpuExecutor:
     """Runs one request on the GB300 engine on its own stream."""
 
-    def __init__(self, device=None, graphs=False):
+    def __init__(self, device=None, graphs=False, workspace_bytes=None):
         import torch
         self.torch = torch
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.graphs = graphs
+        # the batch workspace one request may size its checkpoint interval for
+        # (default an eighth of the device, so several requests run at once)
+        self.workspace_bytes = (int(workspace_bytes) if workspace_bytes else
+                                torch.cuda.get_device_properties(self.device).total_memory // 8)
 
     def plan_for(self, req):
         from .backend import Plan, choose_batch, default_ckpt_k
@@ -136,9 +140,11 @@ class GpuExecutor:
         C = req.batch or choose_batch(shape, req.nt, tx.rows, rx.rows, len(rx.cell), 0, mode,
                                       1 << 62)
         C = min(C, 32)
-        # the backend's default interval (one segment when its stash fits);
-        # the footprint used for admission is this plan's workspace
-        k = default_ckpt_k(shape, req.nt, rx.rows, len(rx.cell), C, mode)
+        # the backend's default interval within this request's workspace share
+        # (one segment when its stash fits); the footprint used for admission
+        # is this plan's workspace
+        k = default_ckpt_k(shape, req.nt, rx.rows, len(rx.cell), C, mode,
+                           budget_bytes=self.workspace_bytes)
         plan = Plan(shape, req.h, req.dt, req.nt, tx, rx, batch=C, ckpt_k=k)
         if not self.graphs:
             plan.set("graphs", 0)

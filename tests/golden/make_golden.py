@@ -3,7 +3,7 @@
 Run in a container that has the reference checkout (it is not needed anywhere
 else; the fixtures are committed):
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout>   (or USCT_REFERENCE=...)
 
 Every case is computed by the reference's Python package ``ringfwi``
 (``simulation/ringfwi/fwi.py``) and, for point elements, also by the
@@ -79,9 +79,12 @@ def _fp_csr(footprints):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("USCT_REFERENCE", ""),
+                    help="the reference checkout (default: $USCT_REFERENCE)")
     ap.add_argument("--only", default="")
     args = ap.parse_args()
+    if not args.ref or not os.path.isdir(os.path.join(args.ref, "simulation")):
+        ap.error("give --ref <reference checkout> or set USCT_REFERENCE")
     only = set(filter(None, args.only.split(",")))
 
     def want(name):

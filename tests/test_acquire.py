@@ -11,7 +11,9 @@ from golden_util import load
 from openusct_gb300 import acquire
 from openusct_gb300.geometry import RingGeometry, ricker
 
-REF = "/root/reference/simulation"
+# the reference's Python package, when USCT_REFERENCE names the checkout
+REF = os.path.join(os.environ.get("USCT_REFERENCE", ""), "simulation") \
+    if os.environ.get("USCT_REFERENCE") else ""
 
 
 def test_peak_frequency_and_fallback_dataset_fields():
@@ -29,7 +31,8 @@ def test_peak_frequency_and_fallback_dataset_fields():
     assert ds.ground_truth["h_m"] == ring.h
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference checkout not present")
+@pytest.mark.skipif(not REF or not os.path.isdir(REF),
+                    reason="USCT_REFERENCE does not name the reference checkout")
 def test_matches_reference_simulate_dataset():
     sys.path.insert(0, REF)
     from ringfwi import acquire as ref_acquire

@@ -116,3 +116,64 @@ def test_320_grid_traces_and_gradient_vs_fp64():
     # is 3.6e-4 of the residual: that, not the kernels, bounds the gradient
     # here (the 192^3 test above holds 1e-4 on a longer time axis)
     assert rel_l2(g32, g64) < 5e-4
+
+
+# ---- the configurations' full time axes against the FP64 oracle -------------
+# The FP32 rounding of the wavefields accumulates over the time steps, so the
+# long axes are the cases that matter.  Shot subsets keep the FP64 runs to a
+# minute or two on the host cores (shots are independent and the gradient is
+# a sum over shots); the oracle checkpoints so its memory stays bounded.
+
+@pytest.mark.slow
+def test_192_full_time_axis_vs_fp64(prob):
+    """192^3, two seeded shots over all nt = 2000 levels: traces <= 1e-5,
+    gradient and misfit <= 1e-4 against the FP64 oracle."""
+    import openusct_gb300.backend as gb
+    rng = np.random.default_rng(1920)
+    sl = sorted(int(s) for s in rng.choice(prob.n_shots, size=2, replace=False))
+    args = (prob.geom, prob.wavelet, prob.dt, prob.h, prob.nt)
+    d64 = oracle.forward_fmc(prob.m_true, *args, None, sl)
+    d32 = gb.forward_fmc(prob.m_true, *args, None, sl)
+    assert rel_l2(d32, d64) < 1e-5
+    J64, g64 = oracle.misfit_and_gradient(prob.m0, *args, d64, None, sl, k=64)
+    J32, g32 = gb.misfit_and_gradient(prob.m0, *args, d64, src_list=sl)
+    assert abs(J32 - J64) <= 1e-4 * J64
+    assert rel_l2(g32, g64) < 1e-4
+
+
+@pytest.mark.slow
+def test_ring2d_full_acquisition_vs_fp64():
+    """The 2D ring configuration in full: 256^2, two seeded discs, all 64
+    shots x 64 receivers over nt = 1500: traces <= 1e-5, gradient and misfit
+    <= 1e-4 against the FP64 oracle."""
+    import openusct_gb300.backend as gb
+    from openusct_gb300 import problems
+    p = problems.ring2d(seed=0)
+    args = (p.geom, p.wavelet, p.dt, p.h, p.nt)
+    d64 = oracle.forward_fmc(p.m_true, *args)
+    d32 = gb.forward_fmc(p.m_true, *args)
+    assert d32.shape == (64, 1500, 64)
+    assert rel_l2(d32, d64) < 1e-5
+    J64, g64 = oracle.misfit_and_gradient(p.m0, *args, d64, k=0)
+    J32, g32 = gb.misfit_and_gradient(p.m0, *args, d64)
+    assert abs(J32 - J64) <= 1e-4 * J64
+    assert rel_l2(g32, g64) < 1e-4
+
+
+@pytest.mark.slow
+def test_320_full_time_axis_vs_fp64():
+    """320^3 (dx = 0.12 mm, 16 x 32 elements), one seeded shot over all
+    nt = 3000 levels: traces <= 1e-5, gradient and misfit <= 1e-4 against the
+    FP64 oracle."""
+    import openusct_gb300.backend as gb
+    from openusct_gb300 import problems
+    p = problems.cylinder3d_large(seed=0)
+    sl = [int(np.random.default_rng(320).integers(p.n_shots))]
+    args = (p.geom, p.wavelet, p.dt, p.h, p.nt)
+    d64 = oracle.forward_fmc(p.m_true, *args, None, sl)
+    d32 = gb.forward_fmc(p.m_true, *args, None, sl)
+    assert rel_l2(d32, d64) < 1e-5
+    J64, g64 = oracle.misfit_and_gradient(p.m0, *args, d64, None, sl, k=64)
+    J32, g32 = gb.misfit_and_gradient(p.m0, *args, d64, src_list=sl)
+    assert abs(J32 - J64) <= 1e-4 * J64
+    assert rel_l2(g32, g64) < 1e-4

@@ -266,8 +266,8 @@ def test_make_sponge_matches_the_reference_and_extends_to_3d():
     for bad in ((8, 80), (64, 80, 5)):
         with pytest.raises(ValueError):
             make_sponge(bad, width=10)
-    ref = "/root/reference/simulation"
-    if os.path.isdir(ref):
+    ref = os.path.join(os.environ.get("USCT_REFERENCE", ""), "simulation")
+    if os.environ.get("USCT_REFERENCE") and os.path.isdir(ref):
         sys.path.insert(0, ref)
         try:
             from ringfwi.solver import make_sponge as ref_sponge
@@ -280,12 +280,12 @@ def test_make_sponge_matches_the_reference_and_extends_to_3d():
 def test_bench_schedule_bytes_and_tail_interval():
     """The pipeline byte count bench.py reports: forward and adjoint on every
     level, the stash on the last segment, the recompute on the others; one
-    segment is 32 C + 24 B per cell-step.  The HBM-sized interval maximises
-    the never-recomputed last segment within the budget."""
+    segment is 32 C + 24 B per cell-step.  The backend's HBM-sized interval
+    maximises the never-recomputed last segment within the budget."""
     import importlib.util
     import os
     from openusct_gb300 import _lib
-    from openusct_gb300.backend import batch_bytes_estimate
+    from openusct_gb300.backend import batch_bytes_estimate, tail_ckpt_k
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(root, "bench.py"))
     bench = importlib.util.module_from_spec(spec)
@@ -300,10 +300,53 @@ def test_bench_schedule_bytes_and_tail_interval():
     assert gn - b64 == cells * 1999 * (12 * C + 4)
     shape, n_rx = (192, 192, 192), 256
     budget = int(0.7 * 284208 * 2 ** 20)
-    k = bench.tail_ckpt_k(shape, nt, n_rx, n_rx, C, _lib.MODE_GRADIENT, budget)
+    k = tail_ckpt_k(shape, nt, n_rx, n_rx, C, _lib.MODE_GRADIENT, budget)
     assert batch_bytes_estimate(shape, nt, n_rx, n_rx, C, k, _lib.MODE_GRADIENT) <= budget
     _, _, tail_k = bench.schedule_bytes(1, C, nt, k, "grad")
     for kk in range(2, nt):
         if batch_bytes_estimate(shape, nt, n_rx, n_rx, C, kk, _lib.MODE_GRADIENT) <= budget:
             assert bench.schedule_bytes(1, C, nt, kk, "grad")[2] <= tail_k
     assert k == 200 and tail_k == 199
+
+
+def test_default_checkpoint_interval_policy():
+    """The public API's interval when none is given: one segment when the whole
+    stash fits the workspace share, else the longest never-recomputed last
+    segment that fits (192^3 / 32 shots: k = 200 within 70 % of a GB300), 0
+    (the engine's memory-saving interval) when nothing fits; chosen once per
+    problem, so a later call under memory pressure keeps the same plan; the
+    fraction can be lowered."""
+    from openusct_gb300 import _lib
+    import openusct_gb300.backend as gb
+    total = 284208 * 2 ** 20
+    G = _lib.MODE_GRADIENT
+    gb._DEFAULT_K.clear()
+    try:
+        assert gb.default_ckpt_k((256, 256), 1500, 64, 64, 64, G, avail=total, total=total) == 1499
+        assert gb.default_ckpt_k((192, 192, 192), 2000, 256, 256, 32, G, avail=total,
+                                 total=total) == 200
+        assert gb.default_ckpt_k((192, 192, 192), 2000, 256, 256, 32, G, avail=10, total=total) == 0
+        assert gb.default_ckpt_k((192, 192, 192), 2000, 256, 256, 32, _lib.MODE_FORWARD) == 0
+        # what the device reported is remembered: a later call under memory
+        # pressure keeps the same interval (and plan)
+        free = [total, total]
+        real = gb._available_bytes
+        gb._available_bytes = lambda: tuple(free)
+        try:
+            assert gb.default_ckpt_k((192, 192, 192), 2000, 256, 256, 32, G) == 200
+            free[0] = 1 << 30
+            assert gb.default_ckpt_k((192, 192, 192), 2000, 256, 256, 32, G) == 200
+        finally:
+            gb._available_bytes = real
+        small = gb.default_ckpt_k((192, 192, 192), 2000, 256, 256, 32, G, avail=total, total=total,
+                                  budget_bytes=150 << 30)
+        assert 0 < small < 200
+        assert gb.batch_bytes_estimate((192, 192, 192), 2000, 256, 256, 32, small, G) <= 150 << 30
+        gb.set_workspace_fraction(0.5)
+        k5 = gb.default_ckpt_k((192, 192, 192), 2000, 256, 256, 32, G, avail=total, total=total)
+        assert 0 < k5 < 200
+        assert gb.batch_bytes_estimate((192, 192, 192), 2000, 256, 256, 32, k5, G) <= 0.5 * total
+        with pytest.raises(ValueError):
+            gb.set_workspace_fraction(1.5)
+    finally:
+        gb.set_workspace_fraction(0.7)
