@@ -196,8 +196,10 @@ def cpu_whole_shot(prob, shot, k, dobs1=None, mode="grad", misfit="l2"):
 
 
 SERVE_STREAM = ("seeded Poisson stream at 20 req/s, 30% gradient / 70% forward, half 2D rings "
-                "(128^2-512^2, 32-128 elements) half 3D cylinders (64^3-128^3, 64-128 elements), "
-                "disc or random-field models, nt = 2.2*2R/1450/dt; HBM budget 150 GB, 6 slots")
+                "(128^2-1024^2, 32-256 elements) half 3D cylinders (96^3-256^3, 64-512 elements), "
+                "disc or random-field models, nt = 2.2*2R/1450/dt (the serving configuration's "
+                "distribution; the first {n} of its 2000 requests); HBM budget 150 GB, 6 slots, "
+                "each request's batch workspace sized within 50 GB")
 
 
 def serve_phase(args):
@@ -212,40 +214,125 @@ def serve_phase(args):
     def dobs_fn(m, geom, wav, dt, h, nt):
         return gb.forward_fmc(m, geom, wav, dt, h, nt)
 
-    reqs = make_stream(args.serve_requests, rate_hz=20.0, seed=11, sizes_2d=(128, 512),
-                       sizes_3d=(64, 128), elements_2d=(32, 128), elements_3d=(64, 128),
+    reqs = make_stream(args.serve_requests, rate_hz=20.0, seed=11, sizes_2d=(128, 1024),
+                       sizes_3d=(96, 256), elements_2d=(32, 256), elements_3d=(64, 512),
                        frac_gradient=0.3, dobs_fn=dobs_fn)
     gb.release()
-    eng = Engine(GpuExecutor(), budget_bytes=150 << 30, max_active=6)
+    budget = 150 << 30
+    eng = Engine(GpuExecutor(workspace_bytes=budget // 3), budget_bytes=budget, max_active=6)
     res = eng.run_stream(reqs)
     st = summarize(res, eng)
-    # plain form: one shot of every request, timed with CUDA events, scaled by its shots
+    # plain form: one shot of every request, the median of three timed calls
+    # (CUDA events), scaled by the request's shot count
     plain_s = 0.0
     for q in reqs:
         one = [0]
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         if q.kind == "forward":
-            gb.plain_forward_fmc(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt, src_list=one)
-            e0.record()
-            gb.plain_forward_fmc(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt, src_list=one)
-            e1.record()
+            call = lambda: gb.plain_forward_fmc(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt,  # noqa
+                                                src_list=one)
         else:
             d1 = q.dobs[:1]
-            gb.plain_misfit_and_gradient(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt, d1, src_list=one)
+            call = lambda: gb.plain_misfit_and_gradient(q.m, q.geom, q.wavelet, q.dt, q.h,  # noqa
+                                                        q.nt, d1, src_list=one)
+        call()
+        runs = []
+        for _ in range(3):
             e0.record()
-            gb.plain_misfit_and_gradient(q.m, q.geom, q.wavelet, q.dt, q.h, q.nt, d1, src_list=one)
+            call()
             e1.record()
-        torch.cuda.synchronize()
-        plain_s += e0.elapsed_time(e1) / 1000.0 * q.n_shots
+            torch.cuda.synchronize()
+            runs.append(e0.elapsed_time(e1) / 1000.0)
+        plain_s += statistics.median(runs) * q.n_shots
     gb.release()
     plain_rate = st.shots / plain_s if plain_s > 0 else None
-    return {"stream": SERVE_STREAM, "requests": st.n, "ok": st.ok, "rejected": st.rejected,
+    return {"stream": SERVE_STREAM.format(n=st.n), "requests": st.n, "ok": st.ok,
+            "rejected": st.rejected, "waited_for_budget": st.waited_for_budget,
+            "budget_gb": budget / 2 ** 30,
             "p50_s": st.p50_s, "p99_s": st.p99_s, "mean_s": st.mean_s,
             "makespan_s": st.makespan_s, "shots": st.shots, "shots_per_s": st.shots_per_s,
             "max_concurrent": st.max_concurrent,
             "peak_reserved_gb": st.peak_reserved_bytes / 2 ** 30,
             "plain_sequential_shots_per_s": plain_rate,
             "speedup_vs_plain_sequential": (st.shots_per_s / plain_rate) if plain_rate else None}
+
+
+GN_WORKLOAD = ("3D Gauss-Newton Hessian-vector product (Born + adjoint), 224^3, dx=0.18mm, 8x32 "
+               "elements (256 shots), nt=2500, FP32, seeded smooth perturbation, 16 shots per "
+               "launch, the backend's default checkpoint interval; one step = one 16-shot batch")
+
+
+def gauss_newton_phase(args):
+    """The Gauss-Newton configuration: the 224^3 Hessian-vector product timed
+    on one 16-shot batch (device-resident inputs, CUDA events), and four
+    Gauss-Newton iterations of the 2D ring problem served as one long-lived
+    device-resident request (arrival -> final model on the host)."""
+    import ctypes
+    import numpy as np
+    import torch
+    import openusct_gb300.backend as gb
+    from openusct_gb300 import _lib, problems
+    from openusct_gb300.geometry import element_csr
+    from openusct_gb300.serve import Engine, GpuExecutor, Request
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    prob = problems.gn3d(seed=0)
+    C = 16
+    shots = list(range(C))
+    tx, rx = element_csr(prob.geom, prob.shape, shots, None)
+    k = gb.default_ckpt_k(prob.shape, prob.nt, rx.rows, len(rx.cell), C, _lib.MODE_BORN)
+    plan = gb.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx, rx, batch=C, ckpt_k=k)
+    lib = _lib.load()
+    s = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    m0 = torch.from_numpy(prob.m0).to(dev)
+    v = torch.from_numpy(prob.v).to(dev)
+    wav = torch.from_numpy(prob.wavelet).to(dev)
+    hv = torch.empty(prob.shape, dtype=torch.float64, device=dev)
+    mws = torch.empty(plan.model_bytes(), dtype=torch.uint8, device=dev)
+    bws = torch.empty(plan.batch_bytes(_lib.MODE_BORN), dtype=torch.uint8, device=dev)
+    call = lambda: _lib.check(lib.usct_gn_hessian_vector_dev(  # noqa: E731
+        plan.handle, P(m0), None, P(wav), P(v), P(hv), None, P(mws), P(bws), sp))
+    call()
+    reps = 2
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(reps):
+        call()
+    e1.record(s)
+    torch.cuda.synchronize()
+    plan.check()
+    t = e0.elapsed_time(e1) / 1000.0 / reps
+    cells = int(np.prod(prob.shape))
+    hbm, peak_kind = _peaks()
+    k_used = plan.info("ckpt_k")
+    sched, _, _ = schedule_bytes(cells, C, prob.nt, k_used, "gn")
+    del bws, mws
+    plan.close()
+    torch.cuda.empty_cache()
+    # four Gauss-Newton iterations of the 2D ring problem as one served request
+    ring = problems.ring2d(seed=0)
+    geo = (ring.geom, ring.wavelet, ring.dt, ring.h, ring.nt)
+    dobs = gb.forward_fmc(ring.m_true, *geo)
+    n = ring.shape[0]
+    yy, xx = np.mgrid[0:n, 0:n].astype(float) * ring.h
+    cc = (n - 1) * ring.h / 2
+    mask = (np.hypot(xx - cc, yy - cc) <= 0.8 * 0.016).astype(float)
+    req = Request(kind="gauss-newton", m=ring.m0.copy(), geom=ring.geom, wavelet=ring.wavelet,
+                  dt=ring.dt, h=ring.h, nt=ring.nt, dobs=dobs, update_mask=mask, n_iter=4,
+                  n_cg=8)
+    gb.release()
+    res = Engine(GpuExecutor(), budget_bytes=150 << 30, max_active=2).run_stream([req])[0]
+    served = {"problem": "2D ring configuration (256^2, 64 shots, nt=1500), 4 iterations, "
+                         "8 CG steps each, radial update mask",
+              "ok": res.ok, "error": res.error, "latency_s": res.latency if res.ok else None,
+              "misfit_history": res.history}
+    return {"workload": GN_WORKLOAD, "value": C / t, "unit": "shots/s", "ms_per_batch": t * 1e3,
+            "ckpt_k": k_used,
+            "pipeline_frac": sched / t / 1e9 / hbm, "peak_kind": peak_kind,
+            "served_gauss_newton_request": served}
 
 
 def run_reference(args, prob, desc_w, mode):
@@ -725,6 +812,13 @@ def main():
                  "speedup_batched_vs_plain": value / world / (1.0 / tp)}
         del pws
 
+    gn = None
+    if rank == 0 and not args.no_serve and args.workload == "grad3d" and not variant:
+        try:
+            gn = gauss_newton_phase(args)
+        except Exception as exc:   # reported, never fatal for the main line
+            gn = {"error": f"{type(exc).__name__}: {exc}"[:300]}
+
     serve = None
     if rank == 0 and not args.no_serve and args.workload == "grad3d" and not variant:
         try:
@@ -785,7 +879,7 @@ def main():
                                   "achieved": pipeline_bytes / (t_ms / 1000.0) / 1e9,
                                   "frac": pipeline_bytes / (t_ms / 1000.0) / 1e9 / hbm,
                                   "model": pipeline_model},
-            "e2e": e2e, "plain": plain, "serve": serve, "cpu_baseline": cpu,
+            "e2e": e2e, "plain": plain, "serve": serve, "gauss_newton": gn, "cpu_baseline": cpu,
             "gpu_launches": launches, "clocks": clk.summary(),
         }
         print(json.dumps(line))

@@ -85,9 +85,12 @@ def _synthetic(shape, nt):
     return IndexGeometry(idx), m, h, dt, ricker(nt, dt, 1e6)
 
 
-def time_kernels(shape, C, nt, tile, what=("fwd", "adj"), reps=2):
+def time_kernels(shape, C, nt, tile, what=("fwd", "adj"), reps=2, tblock=0, tblock_stages=0,
+                 tblock_zchunk=0):
     """Per-launch milliseconds of the forward, Born-forward and adjoint stencils
-    for a tile (``what`` names those timed: "fwd", "born", "adj")."""
+    for a tile (``what`` names those timed: "fwd", "born", "adj").  With
+    ``tblock`` (a two-step tile W*100+H, or 1 for the default) the forward sweep
+    takes two levels per launch and ``fwd_ms`` is per level."""
     import torch
     from .backend import Plan, _ptr, _stream
     geom, m, h, dt, wav = _synthetic(shape, nt)
@@ -99,6 +102,12 @@ def time_kernels(shape, C, nt, tile, what=("fwd", "adj"), reps=2):
                 stages=tile[4] if len(tile) > 4 else None)
     if len(tile) > 5:
         plan.set("stages_adj", int(tile[5]))
+    if tblock_stages:
+        plan.set("tblock_stages", int(tblock_stages))
+    if tblock_zchunk:
+        plan.set("tblock_zchunk", int(tblock_zchunk))
+    if tblock:
+        plan.set("tblock", int(tblock))
     lib = _lib.load()
     dev = torch.device("cuda", torch.cuda.current_device())
     md = torch.from_numpy(m).to(dev)
@@ -160,6 +169,8 @@ def time_kernels(shape, C, nt, tile, what=("fwd", "adj"), reps=2):
     plan.check()
     out["tile"] = [plan.info("tile_x"), plan.info("tile_y"), plan.info("zchunk"),
                    plan.info("variant")] + [int(v) for v in tile[4:6]]
+    if tblock:
+        out["tblock"] = plan.info("tblock")
     plan.close()
     return out
 
@@ -204,10 +215,21 @@ def main():
     ap.add_argument("--tiles", default="")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--store", action="store_true")
+    ap.add_argument("--tblock", default="",
+                    help="two-step forward tiles W*100+H (1 = default), comma-separated")
+    ap.add_argument("--tblock-stages", type=int, default=0)
+    ap.add_argument("--tblock-zchunk", default="0")
     a = ap.parse_args()
     shape = (a.n,) * a.dim
     what = tuple(a.what.split(","))
-    if a.tiles:
+    if a.tblock:
+        t = _parse_tiles(a.tiles)[0] if a.tiles else (0, 0, 0)
+        for tb in [int(v) for v in a.tblock.split(",")]:
+            for zc in [int(v) for v in a.tblock_zchunk.split(",")]:
+                print(json.dumps({"shape": shape, "C": a.batch, "tblock_zchunk": zc,
+                                  **time_kernels(shape, a.batch, a.nt, t, what, a.reps, tb,
+                                                 a.tblock_stages, zc)}))
+    elif a.tiles:
         for t in _parse_tiles(a.tiles):
             print(json.dumps({"shape": shape, "C": a.batch, **time_kernels(shape, a.batch, a.nt,
                                                                            t, what, a.reps)}))

@@ -116,8 +116,7 @@ class Plan:
             self.set("stages", int(stages))
         self._ws = {}
         self.lock = threading.RLock()
-        with _PLANS_LOCK:
-            _LIVE_PLANS.add(self)
+        _register_live(self)
         # launch-bound sizes replay whole batch sweeps as CUDA graphs
         level = int(np.prod(self.shape)) * max(1, self.batch)
         if level <= (1 << 22):
@@ -302,7 +301,7 @@ def _held_workspace_bytes(plan=None, kind=None):
     """Bytes of the workspaces every live plan holds (cached ones, and ones
     evicted from the cache that a caller still uses), not counting ``plan``'s
     workspace of ``kind`` (the one a new allocation replaces)."""
-    with _PLANS_LOCK:
+    with _LIVE_LOCK:
         plans = list(_LIVE_PLANS)
     if plan is not None and plan not in plans:
         plans.append(plan)
@@ -316,6 +315,14 @@ def _held_workspace_bytes(plan=None, kind=None):
 
 _PLANS: "OrderedDict[tuple, Plan]" = OrderedDict()
 _LIVE_PLANS: "weakref.WeakSet[Plan]" = weakref.WeakSet()
+_LIVE_LOCK = threading.Lock()
+
+
+def _register_live(plan):
+    """Count ``plan``'s workspaces against the cap while it is alive.  Its own
+    lock: plans are built while get_plan holds _PLANS_LOCK."""
+    with _LIVE_LOCK:
+        _LIVE_PLANS.add(plan)
 _MAX_PLANS = 8
 _PLANS_LOCK = threading.Lock()
 

@@ -26,7 +26,7 @@ SOURCES = [("usct_engine.cu", "usct_engine.o", []), ("usct_noalloc.cu", "usct_no
            ("usct_invert.cu", "usct_invert.o", []), ("usct_tfm.cu", "usct_tfm.o", [])] + [
     ("usct_tma_inst.cu", f"usct_tma_c{c}.o", [f"-DUSCT_TMA_C={c}"]) for c in TMA_CHANNELS]
 DEPS = ["usct_engine.cu", "usct_noalloc.cu", "usct_invert.cu", "usct_tfm.cu", "usct_tma_inst.cu",
-        "usct_kernels.cuh", "usct_plain.cuh", "usct_tma.cuh", "usct_convert.cuh"]
+        "usct_kernels.cuh", "usct_plain.cuh", "usct_tma.cuh", "usct_tma2.cuh", "usct_convert.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

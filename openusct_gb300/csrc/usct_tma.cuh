@@ -739,4 +739,22 @@ int tma_adjoint(const TmaLaunch& t, const AdjArgs& a, const AdjMaps& mp);
 template <int C>
 void tma_allow_smem(int bytes);
 
+// the two-step forward (usct_tma2.cuh): tile W x H cells, RA / RB ring stages
+struct Fwd2Args;
+struct Fwd2Maps;
+struct TmaLaunch2 {
+    dim3 grid;
+    size_t smem;
+    int RA, RB;
+    cudaStream_t stream;
+    int* err;
+    int w, h;
+};
+template <int C>
+int tma_forward2(const TmaLaunch2& t, const Fwd2Args& a, const Fwd2Maps& mp);
+struct Adj2Args;
+struct Adj2Maps;
+template <int C>
+int tma_adjoint2(const TmaLaunch2& t, const Adj2Args& a, const Adj2Maps& mp);
+
 }  // namespace usct

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "usct_tma.cuh"
+#include "usct_tma2.cuh"
 
 #ifndef USCT_TMA_C
 #error "compile with -DUSCT_TMA_C=<shot channels>"
@@ -36,6 +37,40 @@ int adj_tile(const TmaLaunch& t, const AdjArgs& a, const AdjMaps& mp) {
         return 0;
     } else {
         return -1;
+    }
+}
+
+constexpr int kFwd2Threads = 256;
+
+template <int kC, int W, int H>
+int fwd2_tile(const TmaLaunch2& t, const Fwd2Args& a, const Fwd2Maps& mp) {
+    if constexpr (kC >= 8) {
+        k_forward2_tma<W, H, kC, kFwd2Threads>
+            <<<t.grid, kFwd2Threads, t.smem, t.stream>>>(a, mp, t.RA, t.RB, t.err);
+        return 0;
+    } else {
+        return -1;
+    }
+}
+
+template <int kC, int W, int H>
+int adj2_tile(const TmaLaunch2& t, const Adj2Args& a, const Adj2Maps& mp) {
+    if constexpr (kC >= 8) {
+        k_adjoint2_tma<W, H, kC, kFwd2Threads>
+            <<<t.grid, kFwd2Threads, t.smem, t.stream>>>(a, mp, t.RA, t.RB, t.err);
+        return 0;
+    } else {
+        return -1;
+    }
+}
+
+template <int kC, int W, int H>
+void allow_tile2(int bytes) {
+    if constexpr (kC >= 8) {
+        cudaFuncSetAttribute(k_forward2_tma<W, H, kC, kFwd2Threads>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        cudaFuncSetAttribute(k_adjoint2_tma<W, H, kC, kFwd2Threads>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     }
 }
 
@@ -91,8 +126,38 @@ int tma_adjoint(const TmaLaunch& t, const AdjArgs& a, const AdjMaps& mp) {
     }
 }
 
+// the two-step tiles (key = W * 100 + H): 4x8, 8x4, 8x8, 16x4, 16x8
+template <int kC>
+int tma_forward2(const TmaLaunch2& t, const Fwd2Args& a, const Fwd2Maps& mp) {
+    switch (t.w * 100 + t.h) {
+        case 408: return fwd2_tile<kC, 4, 8>(t, a, mp);
+        case 804: return fwd2_tile<kC, 8, 4>(t, a, mp);
+        case 808: return fwd2_tile<kC, 8, 8>(t, a, mp);
+        case 1604: return fwd2_tile<kC, 16, 4>(t, a, mp);
+        case 1608: return fwd2_tile<kC, 16, 8>(t, a, mp);
+        default: return -1;
+    }
+}
+
+template <int kC>
+int tma_adjoint2(const TmaLaunch2& t, const Adj2Args& a, const Adj2Maps& mp) {
+    switch (t.w * 100 + t.h) {
+        case 408: return adj2_tile<kC, 4, 8>(t, a, mp);
+        case 804: return adj2_tile<kC, 8, 4>(t, a, mp);
+        case 808: return adj2_tile<kC, 8, 8>(t, a, mp);
+        case 1604: return adj2_tile<kC, 16, 4>(t, a, mp);
+        case 1608: return adj2_tile<kC, 16, 8>(t, a, mp);
+        default: return -1;
+    }
+}
+
 template <int kC>
 void tma_allow_smem(int bytes) {
+    allow_tile2<kC, 4, 8>(bytes);
+    allow_tile2<kC, 8, 4>(bytes);
+    allow_tile2<kC, 8, 8>(bytes);
+    allow_tile2<kC, 16, 4>(bytes);
+    allow_tile2<kC, 16, 8>(bytes);
     allow_tile<kC, 32, 4, true>(bytes);
     allow_tile<kC, 32, 8, true>(bytes);
     allow_tile<kC, 64, 2, true>(bytes);
@@ -104,5 +169,7 @@ void tma_allow_smem(int bytes) {
 template int tma_forward<USCT_TMA_C>(const TmaLaunch&, const FwdArgs&, const FwdMaps&, bool);
 template int tma_adjoint<USCT_TMA_C>(const TmaLaunch&, const AdjArgs&, const AdjMaps&);
 template void tma_allow_smem<USCT_TMA_C>(int);
+template int tma_forward2<USCT_TMA_C>(const TmaLaunch2&, const Fwd2Args&, const Fwd2Maps&);
+template int tma_adjoint2<USCT_TMA_C>(const TmaLaunch2&, const Adj2Args&, const Adj2Maps&);
 
 }  // namespace usct

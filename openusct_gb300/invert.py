@@ -228,9 +228,13 @@ class _Evaluator:
 def invert(m0, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, n_iter=15,
            step_frac=0.02, update_mask=None, m_bounds=None, smooth_sigma=1.0, n_linesearch=8,
            verbose=False, backend=None, misfit_type="l2", footprints=None, progress=None,
-           time_weights=None, optimizer="gd", n_cg=8, gn_damp=1e-2):
+           time_weights=None, optimizer="gd", n_cg=8, gn_damp=1e-2, engine_options=None):
     """Device-resident ``fwi.invert``; returns ``(m, history)`` like the reference
-    (``m`` a NumPy array, or a CUDA tensor when ``m0`` is one)."""
+    (``m`` a NumPy array, or a CUDA tensor when ``m0`` is one).
+
+    ``engine_options`` (this backend only): ``batch`` (shots per launch) and
+    ``ckpt_k`` (checkpoint interval) for every gradient and Gauss-Newton call
+    of the Gauss-Newton loop; the default is the backend's own choice."""
     if optimizer in ("gauss-newton", "gn"):
         if misfit_type != "l2":
             raise ValueError("Gauss-Newton is defined for the L2 misfit; "
@@ -257,7 +261,7 @@ def invert(m0, geom, wavelet, dt, h, nt, dobs, sponge=None, src_list=None, n_ite
     if optimizer in ("gauss-newton", "gn"):
         m, history = _gauss_newton(be, ops, m0d, geom, wavelet, dt, h, nt, dobs, sponge, src_list,
                                    n_iter, mask, lo, hi, n_linesearch, verbose, progress,
-                                   footprints, n_cg, gn_damp)
+                                   footprints, n_cg, gn_damp, engine_options)
     else:
         m, history = _descent(be, ops, m0d, geom, wavelet, dt, h, nt, dobs, sponge, src_list,
                               n_iter, step_frac, mask, lo, hi, smooth_sigma, n_linesearch,
@@ -325,10 +329,14 @@ def _descent(be, ops, m0, geom, wavelet, dt, h, nt, dobs, sponge, src_list, n_it
 
 
 def _gauss_newton(be, ops, m0, geom, wavelet, dt, h, nt, dobs, sponge, src_list, n_iter, mask,
-                  lo, hi, n_linesearch, verbose, progress, footprints, n_cg, gn_damp):
+                  lo, hi, n_linesearch, verbose, progress, footprints, n_cg, gn_damp,
+                  engine_options=None):
     """fwi.py:447-532 on the device: CG on (J^T J + mu I) dm = -g, then a
     backtracking line search along dm."""
     kw = dict(footprints=footprints)
+    eo = dict(engine_options or {})
+    kw_mf = dict(batch=eo["batch"]) if "batch" in eo else {}   # misfit takes no interval
+    kw.update(eo)
     m = m0.clone()
     m_try = ops.empty()
     gm, xm, hv = ops.empty(), ops.empty(), ops.empty()
@@ -372,7 +380,7 @@ def _gauss_newton(be, ops, m0, geom, wavelet, dt, h, nt, dobs, sponge, src_list,
         for _ in range(n_linesearch):
             ops.trial(m, step, x, lo, hi, mask, m_try)
             J_try = be.misfit(m_try, geom, wavelet, dt, h, nt, dobs, sponge, src_list, "l2",
-                              footprints)
+                              footprints, **kw_mf)
             if J_try < J:
                 accepted = True
                 break
@@ -385,7 +393,7 @@ def _gauss_newton(be, ops, m0, geom, wavelet, dt, h, nt, dobs, sponge, src_list,
         if progress is not None:
             progress(it + 1, n_iter)
     history.append(be.misfit(m, geom, wavelet, dt, h, nt, dobs, sponge, src_list, "l2",
-                             footprints))
+                             footprints, **kw_mf))
     return m, history
 
 

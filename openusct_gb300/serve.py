@@ -1,7 +1,8 @@
-"""Continuous-batching service for forward and gradient FMC requests.
+"""Continuous-batching service for forward, gradient and Gauss-Newton FMC requests.
 
-Requests of different grids, element counts and kinds (forward-only or L2
-gradient) arrive over time.  The scheduler admits a request as soon as a slot
+Requests of different grids, element counts and kinds (forward-only, L2/GCN
+gradient, or a Gauss-Newton inversion of ``n_iter`` outer iterations served as
+one long-lived request) arrive over time.  The scheduler admits a request as soon as a slot
 is free and its device footprint (model + batch workspaces + its data, from
 the engine's own size queries) fits the HBM budget; requests that do not fit
 wait while later, smaller ones may go ahead; a request larger than the whole
@@ -10,6 +11,12 @@ workspaces and its own CUDA stream, so the batch sweeps of co-admitted
 requests overlap on the device; the request's shots advance C at a time in one
 launch per time step.  Wavefields and checkpoints stay on the device; only the
 request's inputs and its result cross PCIe/C2C.
+
+A Gauss-Newton request runs the device-resident ``invert(optimizer=
+"gauss-newton")`` (fwi.py:434-532) on its own plan, workspace and stream: the
+model, the observed data and every wavefield stay on the device across its
+iterations, and only scalars (misfits, CG dot products) reach the host until
+the final model.
 
 Latency is measured from a request's arrival to its result being on the host;
 ``Stats`` gives p50/p99 and shots/s.  The scheduling logic is independent of
@@ -30,7 +37,7 @@ from . import _lib
 
 @dataclass
 class Request:
-    kind: str                      # "forward" | "gradient"
+    kind: str                      # "forward" | "gradient" | "gauss-newton"
     m: np.ndarray                  # squared slowness on the grid
     geom: object                   # .idx of grid-index tuples
     wavelet: np.ndarray
@@ -43,6 +50,10 @@ class Request:
     sponge: np.ndarray | None = None
     misfit_type: str = "l2"        # gradient requests: "l2" or "gcn"
     time_weights: object = None    # gradient requests: one (nt, n_rx) window per transmit
+    n_iter: int = 4                # gauss-newton requests: outer iterations
+    n_cg: int = 8                  # gauss-newton requests: CG steps per iteration
+    update_mask: np.ndarray | None = None   # gauss-newton requests
+    m_bounds: tuple | None = None           # gauss-newton requests
     arrival: float = 0.0           # seconds after the stream starts
     rid: int = -1
     batch: int | None = None
@@ -72,11 +83,14 @@ class Result:
     traces: np.ndarray | None = None
     J: float | None = None
     g: np.ndarray | None = None
+    m: np.ndarray | None = None          # gauss-newton: the final model
+    history: list | None = None          # gauss-newton: the misfit history
     shots: int = 0
     footprint: int = 0
     t_arrival: float = 0.0
     t_admit: float = 0.0
     t_done: float = 0.0
+    waited_for_budget: bool = False      # a slot was free but its footprint did not fit
 
     @property
     def latency(self):
@@ -88,6 +102,7 @@ class Result:
                 "shots": self.shots, "device_bytes": self.footprint,
                 "t_arrival": self.t_arrival, "t_admit": self.t_admit, "t_done": self.t_done,
                 "queue_s": max(0.0, self.t_admit - self.t_arrival),
+                "waited_for_budget": self.waited_for_budget,
                 "latency_s": self.latency if self.ok else None}
 
 
@@ -104,6 +119,7 @@ class Stats:
     shots_per_s: float
     max_concurrent: int
     peak_reserved_bytes: int
+    waited_for_budget: int = 0
 
     def as_dict(self):
         return dict(self.__dict__)
@@ -116,6 +132,61 @@ def percentile(xs, q):
     k = (len(xs) - 1) * q / 100.0
     lo, hi = int(np.floor(k)), int(np.ceil(k))
     return xs[lo] + (xs[hi] - xs[lo]) * (k - lo)
+
+
+_MODES = {"forward": _lib.MODE_FORWARD, "gradient": _lib.MODE_GRADIENT,
+          "gauss-newton": _lib.MODE_BORN}
+
+
+class _PlanBackend:
+    """The backend protocol of ``invert`` (misfit, misfit_and_gradient,
+    gn_hessian_vector on CUDA tensors) bound to one request's plan, model and
+    batch workspaces (the batch workspace sized for the Born mode, of which the
+    gradient and forward layouts are prefixes), its wavelet, sponge and
+    observed data on the device, and its stream."""
+
+    def __init__(self, plan, mws, bws, wavelet, sponge, dobs, stream):
+        from .backend import _ptr, _stream
+        self.plan, self.P = plan, _ptr
+        self.mws, self.bws, self.w, self.sp, self.dobs = mws, bws, wavelet, sponge, dobs
+        self.stream, self.s = stream, _stream(stream)
+        self.lib = plan._lib
+
+    def _J(self):
+        import torch
+        return torch.zeros(self.plan.n_tx, dtype=torch.float64, device=self.dobs.device)
+
+    def misfit(self, m, *args, **kw):
+        P, p, J = self.P, self.plan, self._J()
+        _lib.check(self.lib.usct_model_prepare(p.handle, P(self.mws), P(m), P(self.sp), None,
+                                               P(self.w), self.s))
+        for b in range(p.nbatch):
+            _lib.check(self.lib.usct_batch_forward(p.handle, P(self.mws), P(self.bws), b,
+                                                   _lib.MODE_FORWARD, None, self.s))
+            _lib.check(self.lib.usct_batch_misfit_tw(p.handle, P(self.bws), b, P(self.dobs),
+                                                     None, 0, P(J), self.s))
+        p.check(self.stream)
+        return float(J.sum().item())
+
+    def misfit_and_gradient(self, m, *args, **kw):
+        import torch
+        P, p, J = self.P, self.plan, self._J()
+        g = torch.empty(p.shape, dtype=torch.float64, device=m.device)
+        _lib.check(self.lib.usct_misfit_and_gradient_dev(
+            p.handle, P(m), P(self.sp), P(self.w), P(self.dobs), P(J), P(g), P(self.mws),
+            P(self.bws), self.s))
+        p.check(self.stream)
+        return float(J.sum().item()), g
+
+    def gn_hessian_vector(self, m, geom, wavelet, dt, h, nt, v, *args, **kw):
+        import torch
+        P, p = self.P, self.plan
+        hv = torch.empty(p.shape, dtype=torch.float64, device=m.device)
+        _lib.check(self.lib.usct_gn_hessian_vector_dev(
+            p.handle, P(m), P(self.sp), P(self.w), P(v.contiguous()), P(hv), None, P(self.mws),
+            P(self.bws), self.s))
+        p.check(self.stream)
+        return hv
 
 
 class GpuExecutor:
@@ -135,11 +206,14 @@ class GpuExecutor:
         from .backend import Plan, choose_batch, default_ckpt_k
         from .geometry import element_csr
         shape = tuple(req.m.shape)
+        if req.kind not in _MODES:
+            raise ValueError(f"unknown request kind {req.kind!r}")
         tx, rx = element_csr(req.geom, shape, req.src_list, req.footprints)
-        mode = _lib.MODE_GRADIENT if req.kind == "gradient" else _lib.MODE_FORWARD
-        C = req.batch or choose_batch(shape, req.nt, tx.rows, rx.rows, len(rx.cell), 0, mode,
-                                      1 << 62)
-        C = min(C, 32)
+        mode = _MODES[req.kind]
+        # the widest batch (<= 32 shots) whose least-memory workspace fits
+        # this request's workspace share
+        C = req.batch or min(32, choose_batch(shape, req.nt, tx.rows, rx.rows, len(rx.cell), 0,
+                                              mode, self.workspace_bytes))
         # the backend's default interval within this request's workspace share
         # (one segment when its stash fits); the footprint used for admission
         # is this plan's workspace
@@ -151,10 +225,14 @@ class GpuExecutor:
         return plan
 
     def footprint(self, req, plan):
-        mode = _lib.MODE_GRADIENT if req.kind == "gradient" else _lib.MODE_FORWARD
+        mode = _MODES[req.kind]
         data = 4 * plan.n_tx * plan.nt * plan.n_rx
         cells = int(np.prod(plan.shape))
-        return plan.model_bytes() + plan.batch_bytes(mode) + data + 16 * cells + (1 << 20)
+        # model-sized FP64 arrays beside the workspaces: the model and gradient;
+        # a Gauss-Newton request's loop holds 13 more (CG vectors, trial model,
+        # mask, bounds)
+        models = 2 if req.kind != "gauss-newton" else 15
+        return plan.model_bytes() + plan.batch_bytes(mode) + data + 8 * models * cells + (1 << 20)
 
     def run(self, req, plan):
         torch = self.torch
@@ -179,6 +257,8 @@ class GpuExecutor:
                     yield b
                     st.synchronize()
 
+            if req.kind == "gauss-newton":
+                return self._gauss_newton(req, plan, m, w, sp, mws, st)
             if req.kind == "forward":
                 bws = torch.empty(plan.batch_bytes(_lib.MODE_FORWARD), dtype=torch.uint8, device=dev)
                 data = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev)
@@ -209,6 +289,30 @@ class GpuExecutor:
             plan.check(st)
             return {"J": float(J.sum().item()), "g": g.cpu().numpy()}
 
+    def _gauss_newton(self, req, plan, m, w, sp, mws, st):
+        """``n_iter`` Gauss-Newton iterations of the device-resident invert on
+        this request's plan; cancellation is checked between iterations."""
+        torch = self.torch
+        from .backend import _to_dev
+        from .invert import invert
+        if req.dobs is None or np.shape(req.dobs) != (plan.n_tx, plan.nt, plan.n_rx):
+            raise ValueError(f"dobs must have shape {(plan.n_tx, plan.nt, plan.n_rx)}")
+        dobs = _to_dev(req.dobs, torch.float32, self.device)
+        bws = torch.empty(plan.batch_bytes(_lib.MODE_BORN), dtype=torch.uint8, device=self.device)
+        be = _PlanBackend(plan, mws, bws, w, sp, dobs, st)
+
+        def progress(done, total):
+            if req.cancelled.is_set():
+                raise Cancelled(f"cancelled after {done} of {total} Gauss-Newton iterations")
+
+        m_out, hist = invert(m, req.geom, req.wavelet, req.dt, req.h, req.nt, dobs,
+                             src_list=req.src_list, n_iter=req.n_iter, optimizer="gauss-newton",
+                             n_cg=req.n_cg, update_mask=req.update_mask, m_bounds=req.m_bounds,
+                             backend=be, progress=progress, footprints=req.footprints)
+        plan.check(st)
+        return {"m": m_out.cpu().numpy(), "history": [float(v) for v in hist],
+                "J": float(hist[-1])}
+
     def release(self, plan):
         plan.close()
 
@@ -236,6 +340,8 @@ class Engine:
             res.traces = out.get("traces")
             res.J = out.get("J")
             res.g = out.get("g")
+            res.m = out.get("m")
+            res.history = out.get("history")
         except Exception as exc:   # the request fails, the service goes on
             res.ok = False
             res.error = f"{type(exc).__name__}: {exc}"[:300]
@@ -324,6 +430,8 @@ class Engine:
                         threads.append(th)
                         th.start()
                     else:
+                        if self.active < self.max_active:   # held back by the budget
+                            results[i].waited_for_budget = True
                         keep.append(item)
                 for item in keep:
                     heapq.heappush(pending, item)
@@ -360,7 +468,8 @@ def summarize(results, engine=None):
                  mean_s=float(np.mean(lat)) if lat else float("nan"), makespan_s=span,
                  shots=shots, shots_per_s=shots / span,
                  max_concurrent=engine.max_concurrent if engine else 0,
-                 peak_reserved_bytes=engine.peak_reserved if engine else 0)
+                 peak_reserved_bytes=engine.peak_reserved if engine else 0,
+                 waited_for_budget=sum(1 for r in results if r.waited_for_budget))
 
 
 # ---------------------------------------------------------------------------

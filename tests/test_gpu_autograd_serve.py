@@ -115,6 +115,47 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
             assert rel_l2(r.g, g) < 1e-5 and abs(r.J - J) <= 1e-9 * abs(J)
 
 
+def test_gauss_newton_request_is_the_same_alone_in_the_mix_and_as_invert():
+    """Four Gauss-Newton iterations served as one long-lived request (the
+    reference's GN-beats-GD setup, test_gauss_newton.py:54-75) give the same
+    final model and misfit history when served alone, when served among
+    overlapping forward and gradient requests, and when run by
+    ``invert(optimizer="gauss-newton")`` through the backend with the same
+    batch width; and the misfit falls as the reference's test demands."""
+    import openusct_gb300.backend as gb
+    from openusct_gb300.invert import invert
+    from openusct_gb300.serve import Engine, GpuExecutor, Request, make_stream
+
+    c = load("gn_vs_gd2d")
+
+    def gn_request(arrival):
+        return Request(kind="gauss-newton", m=c["m0"].copy(), geom=c.geom, wavelet=c.wavelet,
+                       dt=c.dt, h=c.h, nt=c.nt, dobs=c["dobs"], src_list=list(c.src_list),
+                       update_mask=c["mask"], n_iter=4, n_cg=8, arrival=arrival, batch=4)
+
+    def dobs_fn(m, geom, wav, dt, h, nt):
+        return gb.forward_fmc(m, geom, wav, dt, h, nt)
+
+    others = make_stream(5, rate_hz=40.0, seed=5, sizes_2d=(96, 160), sizes_3d=(40, 56),
+                         elements_2d=(16, 32), elements_3d=(16, 32), frac_gradient=0.5,
+                         nt_cap=300, dobs_fn=dobs_fn)
+    mix = others[:2] + [gn_request(others[1].arrival + 0.01)] + others[2:]
+    eng = Engine(GpuExecutor(), budget_bytes=40 << 30, max_active=4)
+    mixed = eng.run_stream(mix)
+    assert all(r.ok for r in mixed), [r.error for r in mixed]
+    assert eng.max_concurrent >= 2
+    served = mixed[2]
+    alone = Engine(GpuExecutor(), budget_bytes=40 << 30, max_active=1).run_stream(
+        [gn_request(0.0)], realtime=False)[0]
+    assert alone.ok
+    assert np.array_equal(served.m, alone.m) and served.history == alone.history
+    m_inv, hist = invert(c["m0"], c.geom, c.wavelet, c.dt, c.h, c.nt, c["dobs"],
+                         src_list=c.src_list, n_iter=4, update_mask=c["mask"],
+                         optimizer="gauss-newton", n_cg=8, engine_options={"batch": 4})
+    assert np.array_equal(served.m, m_inv) and served.history == [float(v) for v in hist]
+    assert served.history[-1] / served.history[0] < 0.05
+
+
 def test_bounded_wait_reports_and_recovers():
     """A TMA stage whose bytes never all arrive: the kernel's bounded wait gives
     up, the error is reported on the host, later launches skip their work, and

@@ -350,3 +350,32 @@ def test_default_checkpoint_interval_policy():
             gb.set_workspace_fraction(1.5)
     finally:
         gb.set_workspace_fraction(0.7)
+
+
+def test_plan_cache_builds_plans_without_deadlock(monkeypatch):
+    """get_plan builds a plan while it holds the cache lock, and a plan
+    registers itself as live on construction: the two must not share a lock
+    (a stand-in plan runs the same registration, under a thread timeout)."""
+    import threading
+    import openusct_gb300.backend as gb
+
+    class Key:
+        def key(self):
+            return ("k",)
+
+    class StandIn:
+        def __init__(self, *a, **k):
+            self._ws = {}
+            gb._register_live(self)
+
+    monkeypatch.setattr(gb, "Plan", StandIn)
+    monkeypatch.setattr(gb, "_PLANS", gb.OrderedDict())
+    monkeypatch.setattr(gb.torch.cuda, "current_device", lambda: 0)
+    out = []
+    th = threading.Thread(target=lambda: out.append(gb.get_plan((8, 8), 1e-3, 1e-7, 10, Key(),
+                                                                Key())), daemon=True)
+    th.start()
+    th.join(timeout=10)
+    assert not th.is_alive(), "get_plan deadlocked"
+    assert isinstance(out[0], StandIn) and out[0] in gb._LIVE_PLANS
+    assert gb._held_workspace_bytes() >= 0

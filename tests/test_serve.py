@@ -82,6 +82,22 @@ def test_smaller_request_passes_a_blocked_head():
     assert rs[2].t_admit < rs[1].t_admit
 
 
+def test_requests_held_back_by_the_budget_are_counted():
+    """A request that finds a free slot but not enough budget waits and is
+    counted as held back by the budget; one that waits for a slot is not."""
+    ex = FakeExecutor()
+    eng = Engine(ex, budget_bytes=100, max_active=2)
+    rs = eng.run_stream([req(60, 0.2, 0.0), req(60, 0.02, 0.01)])
+    assert all(r.ok for r in rs)
+    assert not rs[0].waited_for_budget and rs[1].waited_for_budget
+    assert summarize(rs, eng).waited_for_budget == 1
+    ex2 = FakeExecutor()
+    eng2 = Engine(ex2, budget_bytes=10 ** 9, max_active=1)
+    rs2 = eng2.run_stream([req(1, 0.1, 0.0), req(1, 0.01, 0.01)])
+    assert not any(r.waited_for_budget for r in rs2)
+    assert rs2[1].record()["waited_for_budget"] is False
+
+
 def test_a_failing_request_does_not_stop_the_service():
     ex = FakeExecutor()
     eng = Engine(ex, budget_bytes=100, max_active=2)
