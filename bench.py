@@ -150,7 +150,7 @@ def host_available_bytes():
     return 0
 
 
-def cpu_shot_interval(prob, mode, frac=0.5):
+def cpu_shot_interval(prob, mode, frac=0.65):
     """The FP64 oracle's memory plan for one whole shot on this host: k = 0 --
     the full history of every level, no recompute, the reference core's own
     plan (libuap.hpp:179-186) -- when that history fits ``frac`` of the

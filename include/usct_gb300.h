@@ -73,7 +73,6 @@ extern "C" {
 #define USCT_INFO_LAUNCHES 8     /* kernels launched by this plan so far */
 #define USCT_INFO_VARIANT 9      /* 0 = register-queue stencils, 1 = TMA ring */
 #define USCT_INFO_TBLOCK 10      /* two-step tile W*100+H of the forward sweeps, 0 = off */
-#define USCT_INFO_TBLOCK_ADJ 11  /* 1 = the adjoint sweeps take two levels per launch too */
 
 /* usct_plan_set keys */
 #define USCT_SET_VARIANT 0       /* 0 = register-queue stencils, 1 = TMA-fed ring */
@@ -92,9 +91,7 @@ extern "C" {
 #define USCT_SET_TBLOCK_STAGES 6 /* two-step rings: 10 * (p^{n-1} stages, 3..6) +
                                     (p^{n-2}/S stages, 2..5) */
 #define USCT_SET_TBLOCK_ZCHUNK 7 /* planes per CTA of the two-step launches (0 = default) */
-#define USCT_SET_TBLOCK_ADJ 8    /* with USCT_SET_TBLOCK on: 1 (default where it fits) = the
-                                    adjoint also takes two levels per launch, 0 = one */
-#define USCT_SET_TBLOCK_STAGES_ADJ 9 /* the two-step adjoint's rings, as USCT_SET_TBLOCK_STAGES */
+
 
 /* One-line message describing the last error on this thread ("" if none). */
 const char* usct_last_error(void);

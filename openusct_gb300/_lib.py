@@ -29,10 +29,9 @@ SMOOTH_MAX_RADIUS = 64      # USCT_SMOOTH_MAX_RADIUS
 DOT_WS_DOUBLES = 609        # USCT_DOT_WS_DOUBLES
 
 INFO = {"batch": 0, "nbatch": 1, "ckpt_k": 2, "nseg": 3, "tile_x": 4, "tile_y": 5,
-        "zchunk": 6, "level_floats": 7, "launches": 8, "variant": 9, "tblock": 10,
-        "tblock_adj": 11}
+        "zchunk": 6, "level_floats": 7, "launches": 8, "variant": 9, "tblock": 10}
 SET = {"variant": 0, "stages": 1, "stages_adj": 2, "graphs": 3, "wait_test": 4, "tblock": 5,
-       "tblock_stages": 6, "tblock_zchunk": 7, "tblock_adj": 8, "tblock_stages_adj": 9}
+       "tblock_stages": 6, "tblock_zchunk": 7}
 
 _vp = ctypes.c_void_p
 _i = ctypes.c_int

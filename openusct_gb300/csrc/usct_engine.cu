@@ -118,14 +118,12 @@ struct usct_plan {
     // two time levels per forward launch (usct_tma2.cuh): tile w2 x h2 cells,
     // its own tiling (ntx2 x nty2 tiles, nzc2 chunks of zc2 planes), ring
     // depths and per-tile lists (sources of the tile grown by one cell/row)
-    int tb = 0, tb_adj = 0, w2 = 0, h2 = 0, zc2 = 0, zc2_req = 0, ntx2 = 0, nty2 = 0, nzc2 = 0, ntiles2 = 0;
-    int ra2 = 5, rb2 = 4, ra2a = 4, rb2a = 3;   // forward / adjoint ring depths
+    int tb = 0, w2 = 0, h2 = 0, zc2 = 0, zc2_req = 0, ntx2 = 0, nty2 = 0, nzc2 = 0, ntiles2 = 0;
+    int ra2 = 5, rb2 = 4;
     int* d_sptr2 = nullptr;
     SrcEnt* d_sent2 = nullptr;
     int* d_rptr2 = nullptr;
     RxEnt* d_rent2 = nullptr;
-    int* d_rptr2g = nullptr;   // receivers of each tile grown by one cell/row (adjoint injection)
-    RxEnt* d_rent2g = nullptr;
     int* d_err = nullptr;   // set by a kernel whose bounded wait gave up
     std::unordered_map<uint64_t, CUtensorMap> maps;
     // CUDA graphs of whole batch sweeps, keyed by (op, batch, mode, buffers)
@@ -171,16 +169,11 @@ static size_t tb_smem(const usct_plan* p, bool has_sp) {
     const Fwd2Layout L = fwd2_layout(p->w2, p->h2, p->C, has_sp, p->ra2, p->rb2);
     return (size_t)L.floats * sizeof(float) + (size_t)(p->ra2 + p->rb2) * 8 + 16;
 }
-static size_t tb_smem_adj(const usct_plan* p, bool has_sp) {
-    const Adj2Layout L = adj2_layout(p->w2, p->h2, p->C, has_sp, true, p->ra2a, p->rb2a);
-    return (size_t)L.floats * sizeof(float) + (size_t)(p->ra2a + p->rb2a) * 8 + 16;
-}
+
 
 static void free_tb_lists(usct_plan* p) {
     cudaFree(p->d_sptr2); cudaFree(p->d_sent2); cudaFree(p->d_rptr2); cudaFree(p->d_rent2);
-    cudaFree(p->d_rptr2g); cudaFree(p->d_rent2g);
     p->d_sptr2 = nullptr; p->d_sent2 = nullptr; p->d_rptr2 = nullptr; p->d_rent2 = nullptr;
-    p->d_rptr2g = nullptr; p->d_rent2g = nullptr;
 }
 
 static void free_plan_dev(usct_plan* p) {
@@ -416,7 +409,6 @@ extern "C" int usct_plan_info(const usct_plan* p, int key, int64_t* value) {
         case USCT_INFO_LAUNCHES: *value = p->launches; break;
         case USCT_INFO_VARIANT: *value = p->variant; break;
         case USCT_INFO_TBLOCK: *value = p->tb ? p->w2 * 100 + p->h2 : 0; break;
-        case USCT_INFO_TBLOCK_ADJ: *value = p->tb && p->tb_adj ? 1 : 0; break;
         default: return set_err(USCT_ERR_ARG, "unknown info key %d", key);
     }
     return USCT_OK;
@@ -452,7 +444,6 @@ struct BatchWS {
     float* P[2]; float* rs; float* res; double* jpart; double* gj; float* ck; float* stash; float* L[2];
     float* D[2];
     float* P2[2];   // the second pair of state levels of two-step sweeps
-    float* L2x[2];  // the second pair of adjoint levels of two-step adjoint sweeps
 };
 
 static BatchWS carve_batch(const usct_plan* p, void* base, int mode) {
@@ -478,10 +469,6 @@ static BatchWS carve_batch(const usct_plan* p, void* base, int mode) {
     if (p->tb) {
         w.P2[0] = (float*)c; c += lv;
         w.P2[1] = (float*)c; c += lv;
-        if (mode >= USCT_MODE_GRADIENT) {
-            w.L2x[0] = (float*)c; c += lv;
-            w.L2x[1] = (float*)c; c += lv;
-        }
     }
     return w;
 }
@@ -495,7 +482,7 @@ extern "C" size_t usct_batch_bytes(const usct_plan* p, int mode) {
                al256((size_t)p->n_rx * p->C * sizeof(double));
     if (mode >= USCT_MODE_GRADIENT) b += (2 + 2 * (size_t)p->nseg + (size_t)p->k) * lv;
     if (mode == USCT_MODE_BORN) b += 2 * lv;
-    if (p->tb) b += (mode >= USCT_MODE_GRADIENT ? 4 : 2) * lv;
+    if (p->tb) b += 2 * lv;
     return b;
 }
 
@@ -710,8 +697,7 @@ static size_t stencil_smem(const usct_plan* p, int nfield) {
 
 // ---- tensor maps for the TMA ring -------------------------------------------
 enum MapKind { MK_WF_HALO = 0, MK_WF_OWN = 1, MK_CELL_OWN = 2, MK_CELL_HALO = 3, MK_G_OWN = 4,
-               MK2_A = 5, MK2_B = 6, MK2_S = 7, MK2_S2 = 8, MK2_OWN = 9,
-               MK2_G = 10 };   // MK2_*: the two-step tiles
+               MK2_A = 5, MK2_B = 6, MK2_S = 7 };   // MK2_*: the two-step tiles
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -730,7 +716,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 // Box shapes (innermost first).  Wavefields: 4D {C, nxs, ny, nz} when C >= 4,
 // otherwise 3D {RP, ny, nz}; model cells: 3D {nxs, ny, nz} (float or double).
 static int get_map(usct_plan* p, const void* ptr, int kind, CUtensorMap* out) {
-    const uint64_t key = (uint64_t)(uintptr_t)ptr * 16u + (uint64_t)kind;
+    const uint64_t key = (uint64_t)(uintptr_t)ptr * 8u + (uint64_t)kind;
     auto it = p->maps.find(key);
     if (it != p->maps.end()) { *out = it->second; return USCT_OK; }
     auto enc = encode_fn();
@@ -743,27 +729,20 @@ static int get_map(usct_plan* p, const void* ptr, int kind, CUtensorMap* out) {
     cuuint32_t rank = 3;
     CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     const bool halo = kind == MK_WF_HALO;
-    if (kind == MK2_A || kind == MK2_B || kind == MK2_OWN) {
-        // two-step tiles: the older input level grown by two cells/rows, the
-        // oldest by one, own tiles (the stash) not grown
-        const int grow = kind == MK2_A ? 4 : (kind == MK2_B ? 2 : 0);
+    if (kind == MK2_A || kind == MK2_B) {
+        // two-step tiles: p^{n-1} grown by two cells/rows, p^{n-2} by one
+        const int grow = kind == MK2_A ? 4 : 2;
         rank = 4;
         dims[0] = g.C; dims[1] = g.nxs; dims[2] = g.ny; dims[3] = g.nz;
         strides[0] = (cuuint64_t)g.C * 4; strides[1] = (cuuint64_t)g.RP * 4;
         strides[2] = (cuuint64_t)g.PP * 4;
         box[0] = g.C; box[1] = p->w2 + grow; box[2] = p->h2 + grow; box[3] = 1;
-    } else if (kind == MK2_S || kind == MK2_S2) {
-        // S / sponge of the tile grown by one (MK2_S) or two (MK2_S2) rows, 4
-        // cells wider on each side so the box's x coordinate stays 16-byte
-        // aligned
+    } else if (kind == MK2_S) {
+        // S / sponge of the grown tile, 4 cells wider on each side so the
+        // box's x coordinate stays 16-byte aligned
         dims[0] = g.nxs; dims[1] = g.ny; dims[2] = g.nz;
         strides[0] = (cuuint64_t)g.nxs * 4; strides[1] = (cuuint64_t)g.CPP * 4;
-        box[0] = p->w2 + 8; box[1] = p->h2 + (kind == MK2_S2 ? 4 : 2); box[2] = 1;
-    } else if (kind == MK2_G) {
-        dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;   // the FP64 gradient of the own tile
-        dims[0] = g.nxs; dims[1] = g.ny; dims[2] = g.nz;
-        strides[0] = (cuuint64_t)g.nxs * 8; strides[1] = (cuuint64_t)g.CPP * 8;
-        box[0] = p->w2; box[1] = p->h2; box[2] = 1;
+        box[0] = p->w2 + 8; box[1] = p->h2 + 2; box[2] = 1;
     } else if (kind == MK_WF_HALO || kind == MK_WF_OWN) {
         if (g.C >= 4) {
             rank = 4;
@@ -945,46 +924,6 @@ static int launch_fwd2(usct_plan* p, const Fwd2Args& a0, cudaStream_t s) {
     return USCT_OK;
 }
 
-static int tma_adj2_dispatch(int C, const TmaLaunch2& t, const Adj2Args& a, const Adj2Maps& mp) {
-    switch (C) {
-        case 8: return tma_adjoint2<8>(t, a, mp);
-        case 16: return tma_adjoint2<16>(t, a, mp);
-        case 32: return tma_adjoint2<32>(t, a, mp);
-        case 64: return tma_adjoint2<64>(t, a, mp);
-        default: return -1;
-    }
-}
-
-// one two-step adjoint launch: lam^k and lam^{k-1} from (lam^{k+2}, lam^{k+1})
-static int launch_adj2(usct_plan* p, const Adj2Args& a0, cudaStream_t s) {
-    Adj2Args a = a0;
-    a.wait_test = p->wait_test;
-    a.g = p->geo;
-    a.g.ntiles_x = p->ntx2;
-    a.g.zc = p->zc2;
-    Adj2Maps mp;
-    memset(&mp, 0, sizeof(mp));
-    TRY(get_map(p, a.l1, MK2_A, &mp.L1));
-    TRY(get_map(p, a.S, MK2_S2, &mp.S));
-    TRY(get_map(p, a.l2, MK2_B, &mp.L2));
-    TRY(get_map(p, a.d2a, MK2_OWN, &mp.Da));
-    TRY(get_map(p, a.d2b, MK2_OWN, &mp.Db));
-    if (a.sp) TRY(get_map(p, a.sp, MK2_S, &mp.sp));
-    if (a.gacc) TRY(get_map(p, a.gacc, MK2_G, &mp.g));
-    const Adj2Layout L = adj2_layout(p->w2, p->h2, p->C, a.sp != nullptr, a.gacc != nullptr,
-                                     p->ra2a, p->rb2a);
-    const size_t smem = (size_t)L.floats * sizeof(float) + (size_t)(p->ra2a + p->rb2a) * 8 + 16;
-    TRY(check_smem(smem));
-    const TmaLaunch2 t{dim3(p->ntx2, p->nty2, p->nzc2), smem, p->ra2a, p->rb2a, s, p->d_err, p->w2,
-                       p->h2};
-    if (tma_adj2_dispatch(p->C, t, a, mp) != 0)
-        return set_err(USCT_ERR_ARG, "no two-step adjoint for tile %dx%d with %d shot channels",
-                       p->w2, p->h2, p->C);
-    ++p->launches;
-    CUDA_TRY(cudaGetLastError());
-    return USCT_OK;
-}
-
 template <bool BORN>
 static int launch_fwd(usct_plan* p, const FwdArgs& a, cudaStream_t s) {
     if (p->variant == 1) return launch_fwd_tma<BORN>(p, a, s);
@@ -1114,48 +1053,12 @@ static int tb_configure(usct_plan* p, int w, int h) {
         }
         rptr[ntiles] = (int)q;
     }
-    // receivers of each tile grown by one cell and one row, for the adjoint's
-    // injection on the grown tile: (plane, row, cell) order, and on any one
-    // cell in receiver order (the sort is stable over the j-ordered input)
-    std::vector<std::pair<int, RxEnt>> gtmp;
-    for (int j = 0; j < p->n_rx; ++j)
-        for (int e = p->h_rx_ptr[j]; e < p->h_rx_ptr[j + 1]; ++e) {
-            int z, y, x;
-            unravel(p, p->h_rx_cell[e], z, y, x);
-            for (int yt = std::max(0, (y - h) / h); yt <= std::min(nty - 1, (y + 1) / h); ++yt) {
-                const int ly = y - (yt * h - 1);
-                if (ly < 0 || ly > h + 1) continue;
-                for (int xt = std::max(0, (x - w) / w); xt <= std::min(ntx - 1, (x + 1) / w); ++xt) {
-                    const int lx = x - (xt * w - 1);
-                    if (lx < 0 || lx > w + 1) continue;
-                    gtmp.push_back({xt + ntx * yt, RxEnt{z, ly, lx, e, j, (float)p->h_rx_w[e], 0, 0}});
-                }
-            }
-        }
-    std::stable_sort(gtmp.begin(), gtmp.end(), [](const auto& a, const auto& b2) {
-        if (a.first != b2.first) return a.first < b2.first;
-        if (a.second.z != b2.second.z) return a.second.z < b2.second.z;
-        if (a.second.ly != b2.second.ly) return a.second.ly < b2.second.ly;
-        return a.second.lcell < b2.second.lcell;
-    });
-    std::vector<int> gptr(ntiles + 1, 0);
-    std::vector<RxEnt> gent;
-    {
-        size_t q = 0;
-        for (int tl = 0; tl < ntiles; ++tl) {
-            gptr[tl] = (int)q;
-            while (q < gtmp.size() && gtmp[q].first == tl) { gent.push_back(gtmp[q].second); ++q; }
-        }
-        gptr[ntiles] = (int)q;
-    }
     if (sent.empty()) sent.push_back(SrcEnt{0x7fffffff, 0, 0, 0.f});   // never matched
     if (rent.empty()) rent.push_back(RxEnt{0x7fffffff, 0, 0, 0, 0, 0.f, 0, 0});
-    if (gent.empty()) gent.push_back(RxEnt{0x7fffffff, 0, 0, 0, 0, 0.f, 0, 0});
     free_tb_lists(p);
     int ret;
     if ((ret = upload(&p->d_sptr2, sptr)) != USCT_OK || (ret = upload(&p->d_sent2, sent)) != USCT_OK ||
-        (ret = upload(&p->d_rptr2, rptr)) != USCT_OK || (ret = upload(&p->d_rent2, rent)) != USCT_OK ||
-        (ret = upload(&p->d_rptr2g, gptr)) != USCT_OK || (ret = upload(&p->d_rent2g, gent)) != USCT_OK) {
+        (ret = upload(&p->d_rptr2, rptr)) != USCT_OK || (ret = upload(&p->d_rent2, rent)) != USCT_OK) {
         free_tb_lists(p);
         return ret;
     }
@@ -1215,34 +1118,7 @@ extern "C" int usct_plan_set(usct_plan* p, int key, int64_t value) {
                 return set_err(USCT_ERR_ARG, "two-step tile %d needs %zu B of shared memory", key2,
                                tb_smem(p, true));
             }
-            // the adjoint's rings likewise; where even the shallowest do not fit,
-            // the adjoint keeps one level per launch
-            while (tb_smem_adj(p, true) > (size_t)smem_optin() && (p->ra2a > 3 || p->rb2a > 2)) {
-                if (p->ra2a > 3) --p->ra2a;
-                else --p->rb2a;
-            }
-            p->tb_adj = tb_smem_adj(p, true) <= (size_t)smem_optin() ? 1 : 0;
             p->tb = 1;
-            return USCT_OK;
-        }
-        case USCT_SET_TBLOCK_ADJ:
-            if (value != 0 && value != 1) return set_err(USCT_ERR_ARG, "tblock_adj must be 0 or 1");
-            if (value == 1 && p->tb && tb_smem_adj(p, true) > (size_t)smem_optin())
-                return set_err(USCT_ERR_ARG, "the two-step adjoint does not fit shared memory");
-            p->tb_adj = (int)value;
-            drop_graphs(p);
-            return USCT_OK;
-        case USCT_SET_TBLOCK_STAGES_ADJ: {
-            const int ra = (int)(value / 10), rb = (int)(value % 10);
-            if (ra < 3 || ra > 6 || rb < 2 || rb > 5)
-                return set_err(USCT_ERR_ARG, "two-step adjoint stages: 10 * (3..6) + (2..5)");
-            const int ra0 = p->ra2a, rb0 = p->rb2a;
-            p->ra2a = ra; p->rb2a = rb;
-            if (p->tb && tb_smem_adj(p, true) > (size_t)smem_optin()) {
-                p->ra2a = ra0; p->rb2a = rb0;
-                return set_err(USCT_ERR_ARG, "two-step adjoint rings %d/%d do not fit", ra, rb);
-            }
-            drop_graphs(p);
             return USCT_OK;
         }
         case USCT_SET_TBLOCK_STAGES: {
@@ -1594,9 +1470,6 @@ static int batch_backward_impl(usct_plan* p, void* model_ws, void* batch_ws, int
     CUDA_TRY(cudaMemsetAsync(B.L[0], 0, 2 * lvb, s));
     const int k = p->k, nt = p->nt;
     float* W[2] = {B.P[0], B.P[1]};
-    // two-step adjoint state: lam^{k+2} = lam[li2], lam^{k+1} = lam[li1]
-    float* lam[4] = {B.L[0], B.L[1], B.L2x[0], B.L2x[1]};
-    int li2 = 0, li1 = 1;
     for (int j = p->nseg - 1; j >= 0; --j) {
         const int a0 = j * k;
         const int b1 = std::min(a0 + k, nt - 1);
@@ -1669,54 +1542,6 @@ static int batch_backward_impl(usct_plan* p, void* model_ws, void* batch_ws, int
                 a.r_ent = p->d_rent;
                 TRY(launch_fwd<false>(p, a, s));
             }
-        }
-        if (tb_on(p) && p->tb_adj) {
-            // adjoint levels two at a time within the segment (both stash
-            // levels present); an odd remainder takes one single-step launch
-            for (int kk = b1; kk >= a0 + 1;) {
-                if (kk - 1 >= a0 + 1) {
-                    int o[2], no = 0;
-                    for (int q = 0; q < 4 && no < 2; ++q)
-                        if (q != li2 && q != li1) o[no++] = q;
-                    Adj2Args a{};
-                    a.l1 = lam[li1];
-                    a.l2 = lam[li2];
-                    a.lk1 = lam[o[0]];
-                    a.lk2 = lam[o[1]];
-                    a.S = M.S;
-                    a.sp = p->has_sp ? M.sp : nullptr;
-                    a.d2a = B.stash + (size_t)(kk - a0 - 1) * lvf;
-                    a.d2b = B.stash + (size_t)(kk - a0 - 2) * lvf;
-                    a.gacc = M.g;
-                    a.r_ptr = p->d_rptr2g;
-                    a.r_ent = p->d_rent2g;
-                    a.res1 = B.res + (size_t)kk * p->n_rx * p->C;
-                    a.res2 = B.res + (size_t)(kk - 1) * p->n_rx * p->C;
-                    TRY(launch_adj2(p, a, s));
-                    li2 = o[0];
-                    li1 = o[1];
-                    kk -= 2;
-                } else {
-                    AdjArgs a{};
-                    a.g = p->geo;
-                    a.l1 = lam[li1];
-                    a.l2 = lam[li2];
-                    a.lk = lam[li2];   // in place over lam^{k+2}
-                    a.S = M.S;
-                    a.sp = p->has_sp ? M.sp : nullptr;
-                    a.d2 = B.stash + (size_t)(kk - a0 - 1) * lvf;
-                    a.gacc = M.g;
-                    a.r_ptr = p->d_rptr;
-                    a.r_ent = p->d_rent;
-                    a.res = B.res + (size_t)kk * p->n_rx * p->C;
-                    TRY(launch_adj(p, a, s));
-                    const int t2 = li2;
-                    li2 = li1;
-                    li1 = t2;
-                    kk -= 1;
-                }
-            }
-            continue;
         }
         for (int kk = b1; kk >= a0 + 1; --kk) {
             AdjArgs a{};

@@ -752,9 +752,6 @@ struct TmaLaunch2 {
 };
 template <int C>
 int tma_forward2(const TmaLaunch2& t, const Fwd2Args& a, const Fwd2Maps& mp);
-struct Adj2Args;
-struct Adj2Maps;
-template <int C>
-int tma_adjoint2(const TmaLaunch2& t, const Adj2Args& a, const Adj2Maps& mp);
+
 
 }  // namespace usct

@@ -327,310 +327,4 @@ __global__ void __launch_bounds__(NT, 1)
     }
 }
 
-// ---------------------------------------------------------------------------
-// adjoint, two levels per launch
-// ---------------------------------------------------------------------------
-// From (lam^{k+2}, lam^{k+1}) to (lam^k, lam^{k-1}) with the imaging condition
-// of both levels.  Step A computes lam^k = (2 lam^{k+1} - lam^{k+2}) +
-// L(S lam^{k+1}) (sponge, residual injection) on the tile grown by one cell
-// and one row and keeps q = S lam^k there (the second step's stencil operand)
-// and lam^k on the own cells; step B computes lam^{k-1} on the own cells of
-// plane z-1, stores both levels and adds both imaging terms to the FP64
-// gradient in the single-step order: g = (g + sum_c lam^k d2p^k) +
-// sum_c lam^{k-1} d2p^{k-1}.  Same arithmetic and op order as k_adjoint_tma,
-// so both levels and the gradient are bit-identical to two single steps.
-struct Adj2Args {
-    Geo g;               // with the two-step tiling's ntiles_x and zc
-    const float* l1;     // lam^{k+1}
-    const float* l2;     // lam^{k+2}
-    float* lk1;          // lam^k     (neither l1 nor l2)
-    float* lk2;          // lam^{k-1} (likewise)
-    const float* S;
-    const float* sp;     // sponge (cell layout) or null
-    const float* d2a;    // stash level d2p^k
-    const float* d2b;    // stash level d2p^{k-1}
-    double* gacc;        // FP64 gradient accumulator (cell layout) or null
-    const int* r_ptr;    // [ntiles+1]: receiver entries of each tile grown by one cell/row
-    const RxEnt* r_ent;
-    const float* res1;   // adjoint source of step k: [n_rx][C]
-    const float* res2;   // of step k-1
-    int wait_test;
-};
-
-struct Adj2Maps {
-    CUtensorMap L1, S, L2, Da, Db, sp, g;
-};
-
-struct Adj2Layout {
-    int a_l1, a_stage, b_l2, b_d, o_sp, o_g, b_stage, q_plane, lk_plane, floats;
-};
-__host__ __device__ inline Adj2Layout adj2_layout(int W, int H, int C, bool has_sp, bool has_g,
-                                                  int RA, int RB) {
-    Adj2Layout L{};
-    L.a_l1 = al32((H + 4) * (W + 4) * C);
-    L.a_stage = L.a_l1 + al32((H + 4) * (W + 8));
-    L.b_l2 = al32((H + 2) * (W + 2) * C);
-    L.b_d = al32(H * W * C);
-    L.o_sp = L.b_l2 + 2 * L.b_d;
-    L.o_g = L.o_sp + (has_sp ? al32((H + 2) * (W + 8)) : 0);
-    L.b_stage = L.o_g + (has_g ? al32(2 * H * W) : 0);
-    L.q_plane = L.b_l2;
-    L.lk_plane = L.b_d;
-    L.floats = RA * L.a_stage + RB * L.b_stage + 3 * L.q_plane + 2 * L.lk_plane;
-    return L;
-}
-
-template <int W, int H, int C, int NT>
-__global__ void __launch_bounds__(NT, 1)
-    k_adjoint2_tma(const Adj2Args a, const __grid_constant__ Adj2Maps mp, const int RA,
-                   const int RB, int* err) {
-    static_assert(C >= 4 && W % 4 == 0, "whole cells per float4, 16-byte aligned boxes");
-    static_assert((H * W * C / 4) % 32 == 0, "the second step's items fill whole warps");
-    extern __shared__ __align__(128) float smf[];
-    constexpr int logC = ilog2c(C);
-    constexpr int G = C / 4;                // lanes holding one cell's channels
-    constexpr int AW = (W + 4) * C;
-    constexpr int BW = (W + 2) * C;
-    constexpr int OW = W * C;               // floats per own row
-    constexpr int BH = H + 2;
-    constexpr int SW = W + 8;
-    constexpr int F1 = BW / 4, I1 = BH * F1;
-    constexpr int F2 = OW / 4, I2 = H * F2;
-    constexpr int N1 = (I1 + NT - 1) / NT, N2 = (I2 + NT - 1) / NT;
-    const bool has_sp = a.sp != nullptr;
-    const bool has_g = a.gacc != nullptr;
-    const Adj2Layout L = adj2_layout(W, H, C, has_sp, has_g, RA, RB);
-    float* sA = smf;
-    float* sB = smf + (size_t)RA * L.a_stage;
-    float* sQ = sB + (size_t)RB * L.b_stage;
-    float* sL = sQ + 3 * L.q_plane;
-    uint64_t* barA = reinterpret_cast<uint64_t*>(sL + 2 * L.lk_plane);
-    uint64_t* barB = barA + RA;
-    int* s_abort = reinterpret_cast<int*>(barB + RB);
-
-    const Geo& g = a.g;
-    const int tid = threadIdx.x;
-    const int x0c = blockIdx.x * W, y0 = blockIdx.y * H;
-    const int z0 = blockIdx.z * g.zc;
-    const int z1 = min(z0 + g.zc, g.nz);
-    const int nB = z1 - z0 + 2;
-    const int nA = nB + 2;
-    const float inv_h2 = g.inv_h2;
-
-    const uint32_t bytesA = (uint32_t)((H + 4) * AW * 4 + (H + 4) * SW * 4);
-    const uint32_t bytesB = (uint32_t)(BH * BW * 4 + 2 * H * OW * 4 + (has_sp ? BH * SW * 4 : 0) +
-                                       (has_g ? H * W * 8 : 0));
-    auto issueA = [&](int i, int slot) {   // plane z0-2+i of lam^{k+1} and S (two-cell halo)
-        uint64_t* bar = barA + slot;
-        float* st = sA + (size_t)slot * L.a_stage;
-        mbar_expect_tx(bar, bytesA + ((a.wait_test && i == 0) ? 16u : 0u));
-        tma4(st, &mp.L1, bar, 0, x0c - 2, y0 - 2, z0 - 2 + i);
-        tma3(st + L.a_l1, &mp.S, bar, x0c - 4, y0 - 2, z0 - 2 + i);
-    };
-    auto issueB = [&](int i, int slot) {   // plane z0-1+i of lam^{k+2}, the stash, sponge, g
-        uint64_t* bar = barB + slot;
-        float* st = sB + (size_t)slot * L.b_stage;
-        const int p = z0 - 1 + i;
-        mbar_expect_tx(bar, bytesB);
-        tma4(st, &mp.L2, bar, 0, x0c - 1, y0 - 1, p);
-        tma4(st + L.b_l2, &mp.Da, bar, 0, x0c, y0, p);
-        tma4(st + L.b_l2 + L.b_d, &mp.Db, bar, 0, x0c, y0, p);
-        if (has_sp) tma3(st + L.o_sp, &mp.sp, bar, x0c - 4, y0 - 1, p);
-        if (has_g) tma3(st + L.o_g, &mp.g, bar, x0c, y0, p);
-    };
-
-    if (aborted(err, s_abort)) return;
-    if (tid == 0) {
-        for (int s = 0; s < RA; ++s) mbar_init(barA + s, 1);
-        for (int s = 0; s < RB; ++s) mbar_init(barB + s, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    const int proA = min(RA, nA), proB = min(RB, nB);
-    if (tid == 0) {
-        for (int i = 0; i < proA; ++i) issueA(i, i);
-        for (int i = 0; i < proB; ++i) issueB(i, i);
-    }
-    int issuedA = proA, issuedB = proB;
-
-    // receiver cursors: step A injects on the grown tile from plane z0-1, step B
-    // on the own cells from z0
-    const int tile = blockIdx.x + g.ntiles_x * blockIdx.y;
-    const int re = a.r_ptr[tile + 1];
-    int ri1 = first_at(a.r_ent, a.r_ptr[tile], re, z0 - 1);
-    int ri2 = first_at(a.r_ent, ri1, re, z0);
-    int rnz1 = ri1 < re ? a.r_ent[ri1].z : 0x7fffffff;
-    int rnz2 = ri2 < re ? a.r_ent[ri2].z : 0x7fffffff;
-
-    int sAm = 0, sAc = 1 % RA, sAp = 2 % RA;
-    int wA = 0, wB = 0;
-    uint32_t phA = 0u, phB = 0u;
-    auto waitA = [&]() {
-        const bool r = wait_bar(barA + wA, phA);
-        if (++wA == RA) { wA = 0; phA ^= 1u; }
-        return r;
-    };
-    auto waitB = [&]() {
-        const bool r = wait_bar(barB + wB, phB);
-        if (++wB == RB) { wB = 0; phB ^= 1u; }
-        return r;
-    };
-    int sBc = 0, sBm = RB - 1;
-    int qc3 = 0;   // q plane slot of plane z
-    int lk2s = 0;  // own lam^k plane slot of plane z (z-1: the other)
-    bool ok = waitA();
-    ok = waitA() && ok;
-
-    for (int i = 0; i < nB; ++i) {
-        const int z = z0 - 1 + i;
-        ok = waitA() && ok;
-        ok = waitB() && ok;
-        // ---- step A: lam^k on the grown tile of plane z ----
-        {
-            const float* Am = sA + (size_t)sAm * L.a_stage;
-            const float* Ac = sA + (size_t)sAc * L.a_stage;
-            const float* Ap = sA + (size_t)sAp * L.a_stage;
-            const float* Sm = Am + L.a_l1;
-            const float* Sc = Ac + L.a_l1;
-            const float* Sp = Ap + L.a_l1;
-            const float* Bc = sB + (size_t)sBc * L.b_stage;
-            const float* SPc = Bc + L.o_sp;
-            float* Q = sQ + (size_t)qc3 * L.q_plane;
-            float* LKo = sL + (size_t)lk2s * L.lk_plane;
-            const bool zin = z >= 1 && z <= g.nz - 2;
-            const bool rec = z == rnz1;
-#pragma unroll
-            for (int u = 0; u < N1; ++u) {
-                const int it = tid + u * NT;
-                if (N1 * NT == I1 || it < I1) {
-                    const int r = it / F1;
-                    const int fo = 4 * (it - r * F1);
-                    const int ci = fo >> logC;
-                    const int ao = (r + 1) * AW + C + fo;
-                    const int so = (r + 1) * SW + ci + 3;
-                    const float4 l1c = ld4(Ac + ao);
-                    const float4 qc = mul4(splat4(Sc[so]), l1c);
-                    const float4 xm = mul4(splat4(Sc[so - 1]), ld4(Ac + ao - C));
-                    const float4 xp = mul4(splat4(Sc[so + 1]), ld4(Ac + ao + C));
-                    const float4 ym = mul4(splat4(Sc[so - SW]), ld4(Ac + ao - AW));
-                    const float4 yp = mul4(splat4(Sc[so + SW]), ld4(Ac + ao + AW));
-                    const float4 qm = mul4(splat4(Sm[so]), ld4(Am + ao));
-                    const float4 qp = mul4(splat4(Sp[so]), ld4(Ap + ao));
-                    const float4 l2v = ld4(Bc + r * BW + fo);
-                    const int x = x0c - 1 + ci, y = y0 - 1 + r;
-                    const bool in = zin && x >= 1 && x <= g.nx - 2 && y >= 1 && y <= g.ny - 2;
-                    float4 t = add4(add4(xm, xp), add4(ym, yp));
-                    t = add4(t, add4(qm, qp));
-                    float4 lq = mul4(fma4(splat4(-6.f), qc, t), splat4(inv_h2));
-                    if (!in) lq = f4zero();
-                    float4 lk = add4(fma4(splat4(2.f), l1c, neg4(l2v)), lq);
-                    if (has_sp) lk = mul4(lk, splat4(SPc[r * SW + ci + 3]));
-                    if (__builtin_expect(rec, 0))
-                        lk = inject_residuals(lk, a.r_ent, ri1, re, z, r, fo >> 2, C, a.res1).lk;
-                    st4(Q + r * BW + fo, mul4(splat4(Sc[so]), lk));
-                    if (r >= 1 && r <= H && ci >= 1 && ci <= W)
-                        st4(LKo + (r - 1) * OW + fo - C, lk);
-                }
-            }
-            if (rec) {
-                while (ri1 < re && a.r_ent[ri1].z == z) ++ri1;
-                rnz1 = ri1 < re ? a.r_ent[ri1].z : 0x7fffffff;
-            }
-        }
-        __syncthreads();   // q and the own lam^k of plane z are complete
-        // ---- step B: lam^{k-1} on the own cells of plane zz = z-1 ----
-        if (i >= 2) {
-            const int zz = z - 1;
-            const float* Qm = sQ + (size_t)(qc3 == 2 ? 0 : qc3 + 1) * L.q_plane;   // plane zz-1
-            const float* Qc = sQ + (size_t)(qc3 == 0 ? 2 : qc3 - 1) * L.q_plane;   // plane zz
-            const float* Qp = sQ + (size_t)qc3 * L.q_plane;                        // plane zz+1
-            const float* LKc = sL + (size_t)(lk2s ^ 1) * L.lk_plane;               // lam^k, plane zz
-            const float* Aw = sA + (size_t)sAm * L.a_stage;                         // lam^{k+1}, zz
-            const float* Bm = sB + (size_t)sBm * L.b_stage;
-            const float* Dam = Bm + L.b_l2;
-            const float* Dbm = Dam + L.b_d;
-            const float* SPm = Bm + L.o_sp;
-            const double* Gm = reinterpret_cast<const double*>(Bm + L.o_g);
-            const bool zin = zz >= 1 && zz <= g.nz - 2;
-            const bool rec = zz == rnz2;
-#pragma unroll
-            for (int u = 0; u < N2; ++u) {
-                const int it = tid + u * NT;
-                if (N2 * NT == I2 || it < I2) {
-                    const int r = it / F2;
-                    const int fo = 4 * (it - r * F2);
-                    const int ci = fo >> logC;
-                    const int po = (r + 1) * BW + C + fo;
-                    const float4 qc = ld4(Qc + po);
-                    const float4 xm = ld4(Qc + po - C), xp = ld4(Qc + po + C);
-                    const float4 ym = ld4(Qc + po - BW), yp = ld4(Qc + po + BW);
-                    const float4 qm = ld4(Qm + po), qp = ld4(Qp + po);
-                    const float4 lkc = ld4(LKc + r * OW + fo);
-                    const float4 l1w = ld4(Aw + (r + 2) * AW + 2 * C + fo);
-                    const int x = x0c + ci, y = y0 + r;
-                    const bool in = zin && x >= 1 && x <= g.nx - 2 && y >= 1 && y <= g.ny - 2;
-                    float4 t = add4(add4(xm, xp), add4(ym, yp));
-                    t = add4(t, add4(qm, qp));
-                    float4 lq = mul4(fma4(splat4(-6.f), qc, t), splat4(inv_h2));
-                    if (!in) lq = f4zero();
-                    float4 lk = add4(fma4(splat4(2.f), lkc, neg4(l1w)), lq);
-                    if (has_sp) lk = mul4(lk, splat4(SPm[(r + 1) * SW + ci + 4]));
-                    if (__builtin_expect(rec, 0))
-                        lk = inject_residuals(lk, a.r_ent, ri2, re, zz, r + 1, (fo + C) >> 2, C,
-                                              a.res2).lk;
-                    const bool own = y < g.ny && x < g.nxs;
-                    if (own) {
-                        const long long go = (long long)zz * g.PP + (long long)y * g.RP +
-                                             (long long)x * C + (fo & (C - 1));
-                        st4(a.lk1 + go, lkc);
-                        st4(a.lk2 + go, lk);
-                    }
-                    if (has_g) {
-                        const float4 p1 = own ? mul4(lkc, ld4(Dam + r * OW + fo)) : f4zero();
-                        const float4 p2 = own ? mul4(lk, ld4(Dbm + r * OW + fo)) : f4zero();
-                        float s1 = (p1.x + p1.y) + (p1.z + p1.w);
-                        float s2 = (p2.x + p2.y) + (p2.z + p2.w);
-#pragma unroll
-                        for (int o = 1; o < G; o <<= 1) {
-                            s1 = s1 + __shfl_xor_sync(0xffffffffu, s1, o);
-                            s2 = s2 + __shfl_xor_sync(0xffffffffu, s2, o);
-                        }
-                        if (own && (tid & (G - 1)) == 0) {
-                            const double g1 = Gm[r * W + ci] + (double)s1;
-                            a.gacc[(long long)zz * g.CPP + (long long)y * g.nxs + x] = g1 + (double)s2;
-                        }
-                    }
-                }
-            }
-            if (rec) {
-                while (ri2 < re && a.r_ent[ri2].z == zz) ++ri2;
-                rnz2 = ri2 < re ? a.r_ent[ri2].z : 0x7fffffff;
-            }
-        }
-        ok = __syncthreads_and(ok) != 0;
-        if (!ok) break;
-        if (tid == 0) {
-            fence_proxy_async();
-            if (i + RA < nA) issueA(i + RA, sAm);
-            if (i >= 1 && i - 1 + RB < nB) issueB(i - 1 + RB, sBm);
-        }
-        if (i + RA < nA) issuedA = i + RA + 1;
-        if (i >= 1 && i - 1 + RB < nB) issuedB = i - 1 + RB + 1;
-        sAm = sAc;
-        sAc = sAp;
-        if (++sAp == RA) sAp = 0;
-        sBm = sBc;
-        if (++sBc == RB) sBc = 0;
-        if (++qc3 == 3) qc3 = 0;
-        lk2s ^= 1;
-    }
-    if (!ok) {
-        if (tid == 0) atomicExch(err, 1);
-        for (int i = (issuedA > RA ? issuedA - RA : 0); i < issuedA; ++i)
-            (void)wait_stage(barA, i, RA);
-        for (int i = (issuedB > RB ? issuedB - RB : 0); i < issuedB; ++i)
-            (void)wait_stage(barB, i, RB);
-    }
-}
-
 }  // namespace usct

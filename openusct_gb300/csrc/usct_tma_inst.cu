@@ -54,22 +54,9 @@ int fwd2_tile(const TmaLaunch2& t, const Fwd2Args& a, const Fwd2Maps& mp) {
 }
 
 template <int kC, int W, int H>
-int adj2_tile(const TmaLaunch2& t, const Adj2Args& a, const Adj2Maps& mp) {
-    if constexpr (kC >= 8) {
-        k_adjoint2_tma<W, H, kC, kFwd2Threads>
-            <<<t.grid, kFwd2Threads, t.smem, t.stream>>>(a, mp, t.RA, t.RB, t.err);
-        return 0;
-    } else {
-        return -1;
-    }
-}
-
-template <int kC, int W, int H>
 void allow_tile2(int bytes) {
     if constexpr (kC >= 8) {
         cudaFuncSetAttribute(k_forward2_tma<W, H, kC, kFwd2Threads>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        cudaFuncSetAttribute(k_adjoint2_tma<W, H, kC, kFwd2Threads>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     }
 }
@@ -140,18 +127,6 @@ int tma_forward2(const TmaLaunch2& t, const Fwd2Args& a, const Fwd2Maps& mp) {
 }
 
 template <int kC>
-int tma_adjoint2(const TmaLaunch2& t, const Adj2Args& a, const Adj2Maps& mp) {
-    switch (t.w * 100 + t.h) {
-        case 408: return adj2_tile<kC, 4, 8>(t, a, mp);
-        case 804: return adj2_tile<kC, 8, 4>(t, a, mp);
-        case 808: return adj2_tile<kC, 8, 8>(t, a, mp);
-        case 1604: return adj2_tile<kC, 16, 4>(t, a, mp);
-        case 1608: return adj2_tile<kC, 16, 8>(t, a, mp);
-        default: return -1;
-    }
-}
-
-template <int kC>
 void tma_allow_smem(int bytes) {
     allow_tile2<kC, 4, 8>(bytes);
     allow_tile2<kC, 8, 4>(bytes);
@@ -170,6 +145,5 @@ template int tma_forward<USCT_TMA_C>(const TmaLaunch&, const FwdArgs&, const Fwd
 template int tma_adjoint<USCT_TMA_C>(const TmaLaunch&, const AdjArgs&, const AdjMaps&);
 template void tma_allow_smem<USCT_TMA_C>(int);
 template int tma_forward2<USCT_TMA_C>(const TmaLaunch2&, const Fwd2Args&, const Fwd2Maps&);
-template int tma_adjoint2<USCT_TMA_C>(const TmaLaunch2&, const Adj2Args&, const Adj2Maps&);
 
 }  // namespace usct
