@@ -131,7 +131,7 @@ class Plan:
         t = self._ws.get(kind)
         if t is not None and t.numel() >= nbytes:
             return t
-        t = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+        t = _alloc_bytes(nbytes, device)
         total = torch.cuda.get_device_properties(device).total_memory
         if nbytes <= total // 8 and \
                 _held_workspace_bytes(self, kind) + nbytes <= total // WS_HOLD_DIV:
@@ -371,8 +371,20 @@ def _setup(m, geom, h, dt, nt, src_list, footprints, mode, batch, ckpt_k, tile):
     return get_plan(shape, h, dt, nt, tx, rx, batch, ckpt_k or 0, *tile)
 
 
+def _alloc_bytes(nbytes, device):
+    """A byte buffer on the device.  The interval a gradient sizes for itself
+    counts the blocks torch has cached but not in use as available; one large
+    workspace cannot be carved from them, so on running out they are handed
+    back to the driver and the allocation is tried once more."""
+    try:
+        return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+    except torch.cuda.OutOfMemoryError:
+        torch.cuda.empty_cache()
+        return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+
+
 def _workspace(nbytes, device):
-    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+    return _alloc_bytes(nbytes, device)
 
 
 def _out(x, like):

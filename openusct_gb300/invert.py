@@ -171,9 +171,8 @@ class _Evaluator:
         # workspaces of its own, not the plan's shared ones: the kept forward
         # state must survive other calls on the same (cached) plan between
         # a trial and its gradient
-        self.mws = torch.empty(max(p.model_bytes(), 256), dtype=torch.uint8, device=dev)
-        self.bws = torch.empty(max(p.batch_bytes(_lib.MODE_GRADIENT), 256), dtype=torch.uint8,
-                               device=dev)
+        self.mws = gb._alloc_bytes(p.model_bytes(), dev)
+        self.bws = gb._alloc_bytes(p.batch_bytes(_lib.MODE_GRADIENT), dev)
         self.single = p.nbatch == 1
         # the model tensor whose forward state the workspaces hold.  The
         # caller must not change that tensor before asking for its gradient
