@@ -198,7 +198,7 @@ def cpu_whole_shot(prob, shot, k, dobs1=None, mode="grad", misfit="l2"):
 SERVE_STREAM = ("seeded Poisson stream at 20 req/s, 30% gradient / 70% forward, half 2D rings "
                 "(128^2-1024^2, 32-256 elements) half 3D cylinders (96^3-256^3, 64-512 elements), "
                 "disc or random-field models, nt = 2.2*2R/1450/dt (the serving configuration's "
-                "distribution; the first {n} of its 2000 requests); HBM budget 150 GB, 6 slots, "
+                "distribution; the first {n} of its 2000 requests); HBM budget 150 GB, 12 slots, "
                 "each request's batch workspace sized within 50 GB")
 
 
@@ -219,7 +219,7 @@ def serve_phase(args):
                        frac_gradient=0.3, dobs_fn=dobs_fn)
     gb.release()
     budget = 150 << 30
-    eng = Engine(GpuExecutor(workspace_bytes=budget // 3), budget_bytes=budget, max_active=6)
+    eng = Engine(GpuExecutor(workspace_bytes=budget // 3), budget_bytes=budget, max_active=12)
     res = eng.run_stream(reqs)
     st = summarize(res, eng)
     # plain form: one shot of every request, the median of three timed calls
