@@ -248,6 +248,7 @@ def serve_phase(args):
     plain_rate = st.shots / plain_s if plain_s > 0 else None
     return {"stream": SERVE_STREAM.format(n=st.n), "requests": st.n, "ok": st.ok,
             "rejected": st.rejected, "waited_for_budget": st.waited_for_budget,
+            "merged_into_shared_launches": st.merged,
             "budget_gb": budget / 2 ** 30,
             "p50_s": st.p50_s, "p99_s": st.p99_s, "mean_s": st.mean_s,
             "makespan_s": st.makespan_s, "shots": st.shots, "shots_per_s": st.shots_per_s,

@@ -129,6 +129,19 @@ int usct_plan_set(usct_plan* plan, int key, int64_t value);
  * for its tensor copies (bounded waits; USCT_ERR_CUDA), then clear the flag. */
 int usct_plan_check(usct_plan* plan, void* stream);
 
+/* Per-channel models (no counterpart in the reference: its core runs one shot
+ * at a time on one model).  Shots of several forward requests on different
+ * models of the same grid, h, dt, nt and wavelet share one plan, so they
+ * advance in one launch: transmit t uses model model_of_tx[t] (host array of
+ * n_tx entries, each < n_models).  Needs the TMA variant, >= 4 shot channels,
+ * one level per launch, no sponge; forward sweeps only (USCT_MODE_FORWARD).
+ * Call before the plan's first sweep: it grows usct_model_bytes by one
+ * wavefield level per batch (S in the wavefields' layout). */
+int usct_plan_set_channel_models(usct_plan* plan, int n_models, const int* model_of_tx);
+/* The per-channel model S from n_models device FP64 models [n_models][cells]
+ * and the FP64 wavelet, for a plan with per-channel models. */
+int usct_model_prepare_channels(usct_plan* plan, void* model_ws, const double* models,
+                                const double* wavelet, void* stream);
 /* Bytes of the model workspace (S, sponge, v/m, wavelet, FP64 gradient). */
 size_t usct_model_bytes(const usct_plan* plan);
 /* Bytes of one batch workspace for a USCT_MODE_*. */

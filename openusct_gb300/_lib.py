@@ -84,6 +84,8 @@ SIGNATURES = {
                                       _dp]),
     "usct_misfit_and_gradient_mt": (_i, [_dp, _ip, _i, _d, _d, _i, _ip, _i, _ip, _i, _dp, _dp,
                                          _dp, _i, _dp]),
+    "usct_plan_set_channel_models": (_i, [_vp, _i, _ip]),
+    "usct_model_prepare_channels": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "usct_forward_fmc_noalloc": (_i, [_i, _ip, _d, _d, _i, _i, _ip, _lp, _dp, _i, _ip, _lp, _dp,
                                       _vp, _vp, _vp, _vp, _vp]),
 }

@@ -124,6 +124,10 @@ struct usct_plan {
     SrcEnt* d_sent2 = nullptr;
     int* d_rptr2 = nullptr;
     RxEnt* d_rent2 = nullptr;
+    // every shot channel on its own model (co-admitted requests in one launch):
+    // transmit t uses model d_tx_model[t] of n_models
+    int pcs = 0, n_models = 0;
+    int* d_tx_model = nullptr;
     int* d_err = nullptr;   // set by a kernel whose bounded wait gave up
     std::unordered_map<uint64_t, CUtensorMap> maps;
     // CUDA graphs of whole batch sweeps, keyed by (op, batch, mode, buffers)
@@ -178,6 +182,8 @@ static void free_tb_lists(usct_plan* p) {
 
 static void free_plan_dev(usct_plan* p) {
     free_tb_lists(p);
+    cudaFree(p->d_tx_model);
+    p->d_tx_model = nullptr;
     cudaFree(p->d_sptr); cudaFree(p->d_sent); cudaFree(p->d_rptr); cudaFree(p->d_rent);
     cudaFree(p->d_rxptr); cudaFree(p->d_tx_cell); cudaFree(p->d_tx_w); cudaFree(p->d_rx_cell);
     cudaFree(p->d_err);
@@ -419,6 +425,7 @@ extern "C" int usct_plan_info(const usct_plan* p, int key, int64_t* value) {
 // ---------------------------------------------------------------------------
 struct ModelWS {
     float* S; float* sp; float* vm; float* wav; double* g;
+    float* Spc;   // per-channel models: S of every batch in the wavefields' layout
 };
 static const int JBLK = 64;   // gather blocks (per-block FP64 misfit partials)
 
@@ -430,14 +437,16 @@ static ModelWS carve_model(const usct_plan* p, void* base) {
     m.sp = (float*)c; c += cf;
     m.vm = (float*)c; c += cf;
     m.wav = (float*)c; c += al256((size_t)p->nt * sizeof(float));
-    m.g = (double*)c;
+    m.g = (double*)c; c += al256(p->cells_p * sizeof(double));
+    m.Spc = p->pcs ? (float*)c : nullptr;
     return m;
 }
 
 extern "C" size_t usct_model_bytes(const usct_plan* p) {
     if (!p) return 0;
     return 3 * al256(p->cells_p * sizeof(float)) + al256((size_t)p->nt * sizeof(float)) +
-           al256(p->cells_p * sizeof(double));
+           al256(p->cells_p * sizeof(double)) +
+           (p->pcs ? (size_t)p->nbatch * al256(p->LV * sizeof(float)) : 0);
 }
 
 struct BatchWS {
@@ -505,6 +514,28 @@ __global__ void k_prepare(const double* __restrict__ m, const double* __restrict
         } else {
             S[i] = 0.f; spo[i] = 0.f; vm[i] = 0.f;
         }
+    }
+}
+
+// S of every batch in the wavefields' layout [b][z][y][x][c] from per-transmit
+// models: transmit t = b*C + c uses models[tx_model[t]]; channels past the last
+// transmit and padded cells get 0 (their fields stay 0).
+__global__ void k_prepare_channels(const double* __restrict__ models, const int* __restrict__ tx_model,
+                                   float* Spc, double dt2, int nx, int nxs, int C, int logC,
+                                   int n_tx, long long ncp, long long total) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i & (C - 1));
+        const long long rest = i >> logC;           // (b, cell)
+        const long long cell = rest % ncp;
+        const int t = (int)(rest / ncp) * C + c;
+        const int x = (int)(cell % nxs);
+        float v = 0.f;
+        if (t < n_tx && x < nx) {
+            const long long u = (cell / nxs) * nx + x;
+            v = (float)(dt2 / models[(long long)tx_model[t] * (ncp / nxs) * nx + u]);
+        }
+        Spc[i] = v;
     }
 }
 
@@ -809,15 +840,15 @@ static void init_tma_attributes() {
 
 // the per-C launchers of usct_tma_inst.cu: 0 = launched, -1 = no kernel
 static int tma_fwd_dispatch(int C, const TmaLaunch& t, const FwdArgs& a, const FwdMaps& mp,
-                            bool born) {
+                            bool born, bool pcs) {
     switch (C) {
-        case 1: return tma_forward<1>(t, a, mp, born);
-        case 2: return tma_forward<2>(t, a, mp, born);
-        case 4: return tma_forward<4>(t, a, mp, born);
-        case 8: return tma_forward<8>(t, a, mp, born);
-        case 16: return tma_forward<16>(t, a, mp, born);
-        case 32: return tma_forward<32>(t, a, mp, born);
-        case 64: return tma_forward<64>(t, a, mp, born);
+        case 1: return tma_forward<1>(t, a, mp, born, pcs);
+        case 2: return tma_forward<2>(t, a, mp, born, pcs);
+        case 4: return tma_forward<4>(t, a, mp, born, pcs);
+        case 8: return tma_forward<8>(t, a, mp, born, pcs);
+        case 16: return tma_forward<16>(t, a, mp, born, pcs);
+        case 32: return tma_forward<32>(t, a, mp, born, pcs);
+        case 64: return tma_forward<64>(t, a, mp, born, pcs);
         default: return -1;
     }
 }
@@ -840,9 +871,10 @@ static int launch_fwd_tma(usct_plan* p, const FwdArgs& a0, cudaStream_t s) {
     a.wait_test = p->wait_test;
     FwdMaps mp;
     memset(&mp, 0, sizeof(mp));
+    const bool pcs = p->pcs && !BORN;
     TRY(get_map(p, a.pc, MK_WF_HALO, &mp.pc));
     TRY(get_map(p, a.pp, MK_WF_OWN, &mp.pp));
-    TRY(get_map(p, a.S, MK_CELL_OWN, &mp.S));
+    TRY(get_map(p, a.S, pcs ? MK_WF_OWN : MK_CELL_OWN, &mp.S));
     if (a.sp) TRY(get_map(p, a.sp, MK_CELL_OWN, &mp.sp));
     if (BORN) {
         TRY(get_map(p, a.dc, MK_WF_HALO, &mp.dc));
@@ -850,12 +882,13 @@ static int launch_fwd_tma(usct_plan* p, const FwdArgs& a0, cudaStream_t s) {
         TRY(get_map(p, a.vm, MK_CELL_OWN, &mp.vm));
     }
     const int R = BORN ? p->stages_born : p->stages_fwd;
-    const FwdStage L = fwd_stage(p->txv, p->ty, p->ndim == 3, BORN, p->C, p->logC, a.sp != nullptr);
+    const FwdStage L = fwd_stage(p->txv, p->ty, p->ndim == 3, BORN, p->C, p->logC, a.sp != nullptr,
+                                 pcs);
     const size_t smem = (size_t)R * L.floats * sizeof(float) + (size_t)R * 8 + 16;
     TRY(check_smem(smem));
     const TmaLaunch t{dim3(p->ntx_t, p->nty_t, p->nzc), smem, R, s, p->d_err, p->txv, p->ty,
                       p->ndim == 3};
-    if (tma_fwd_dispatch(p->C, t, a, mp, BORN) != 0)
+    if (tma_fwd_dispatch(p->C, t, a, mp, BORN, pcs) != 0)
         return set_err(USCT_ERR_ARG, "no %dD TMA kernel for tile %dx%d with %d shot channels",
                        p->ndim, p->txv, p->ty, p->C);
     ++p->launches;
@@ -927,6 +960,7 @@ static int launch_fwd2(usct_plan* p, const Fwd2Args& a0, cudaStream_t s) {
 template <bool BORN>
 static int launch_fwd(usct_plan* p, const FwdArgs& a, cudaStream_t s) {
     if (p->variant == 1) return launch_fwd_tma<BORN>(p, a, s);
+    if (p->pcs) return set_err(USCT_ERR_ARG, "per-channel models need the TMA variant");
     const dim3 grid(p->ntx_t, p->nty_t, p->nzc);
     const size_t smem = stencil_smem(p, BORN ? 2 : 1);
     const int key = p->txv * 1000 + p->ty;
@@ -1184,6 +1218,52 @@ extern "C" int usct_model_prepare(usct_plan* p, void* model_ws, const double* m,
     return USCT_OK;
 }
 
+extern "C" int usct_plan_set_channel_models(usct_plan* p, int n_models, const int* model_of_tx) {
+    if (!p || !model_of_tx) return set_err(USCT_ERR_ARG, "null argument");
+    if (n_models < 1) return set_err(USCT_ERR_ARG, "need at least one model");
+    if (p->launches > 0)
+        return set_err(USCT_ERR_STATE, "set per-channel models before the plan's first sweep "
+                                       "(they change usct_model_bytes)");
+    if (p->variant != 1 || p->C < 4 || p->tb)
+        return set_err(USCT_ERR_ARG, "per-channel models need the TMA variant, >= 4 shot channels "
+                                     "and one level per launch");
+    for (int t = 0; t < p->n_tx; ++t)
+        if (model_of_tx[t] < 0 || model_of_tx[t] >= n_models)
+            return set_err(USCT_ERR_ARG, "transmit %d names model %d of %d", t, model_of_tx[t],
+                           n_models);
+    cudaFree(p->d_tx_model);
+    p->d_tx_model = nullptr;
+    TRY(upload(&p->d_tx_model, std::vector<int>(model_of_tx, model_of_tx + p->n_tx)));
+    p->pcs = 1;
+    p->n_models = n_models;
+    drop_graphs(p);
+    return USCT_OK;
+}
+
+extern "C" int usct_model_prepare_channels(usct_plan* p, void* model_ws, const double* models,
+                                           const double* wavelet, void* stream) {
+    Range range_("usct_model_prepare_channels");
+    if (!p || !model_ws || !models || !wavelet) return set_err(USCT_ERR_ARG, "null argument");
+    if (!p->pcs) return set_err(USCT_ERR_STATE, "the plan has no per-channel models");
+    cudaStream_t s = (cudaStream_t)stream;
+    ModelWS M = carve_model(p, model_ws);
+    const long long lvf = (long long)(al256(p->LV * sizeof(float)) / sizeof(float));
+    // batch b's S starts at b * lvf (a level each, 256-byte aligned)
+    for (int b = 0; b < p->nbatch; ++b) {
+        k_prepare_channels<<<grid1d((long long)p->LV), 256, 0, s>>>(
+            models, p->d_tx_model + (size_t)b * p->C, M.Spc + (size_t)b * lvf, p->dt * p->dt,
+            p->geo.nx, p->geo.nxs, p->C, p->logC, std::min(p->C, p->n_tx - b * p->C),
+            (long long)p->cells_p, (long long)p->LV);
+        ++p->launches;
+    }
+    k_wavelet<<<(p->nt + 255) / 256, 256, 0, s>>>(wavelet, M.wav, p->nt);
+    ++p->launches;
+    CUDA_TRY(cudaGetLastError());
+    p->has_sp = false;
+    p->has_vm = false;
+    return USCT_OK;
+}
+
 extern "C" int usct_model_gradient(usct_plan* p, void* model_ws, const double* m, double* grad,
                                    void* stream) {
     Range range_("usct_model_gradient");
@@ -1258,6 +1338,8 @@ extern "C" int usct_batch_forward(usct_plan* p, const void* model_ws, void* batc
     if (mode < USCT_MODE_FORWARD || mode > USCT_MODE_BORN) return set_err(USCT_ERR_ARG, "bad mode");
     if (mode == USCT_MODE_BORN && !p->has_vm)
         return set_err(USCT_ERR_STATE, "Born sweep needs a model prepared with v");
+    if (p->pcs && mode != USCT_MODE_FORWARD)
+        return set_err(USCT_ERR_ARG, "a plan with per-channel models runs forward sweeps only");
     cudaStream_t s = (cudaStream_t)stream;
     // the sponge choice is baked into captured launches: key on it too
     const void* k2 = (const void*)((uintptr_t)traces ^ (p->has_sp ? (uintptr_t)1 : 0));
@@ -1351,6 +1433,7 @@ static int batch_forward_impl(usct_plan* p, const void* model_ws, void* batch_ws
         return gather(p, B, b, traces, nullptr, 0, s);
     }
     const size_t lvf = lvb / sizeof(float);
+    const float* Sb = p->pcs ? M.Spc + (size_t)b * lvf : M.S;   // this batch's S
     const int k = p->k, nt = p->nt;
     const int al = (p->nseg - 1) * k;
     for (int n = 1; n < nt; ++n) {
@@ -1359,7 +1442,7 @@ static int batch_forward_impl(usct_plan* p, const void* model_ws, void* batch_ws
         a.pc = B.P[(n - 1) & 1];
         a.pp = B.P[n & 1];
         a.pn = B.P[n & 1];
-        a.S = M.S;
+        a.S = Sb;
         a.sp = p->has_sp ? M.sp : nullptr;
         a.wav = M.wav;
         a.n = n;

@@ -52,8 +52,9 @@ __host__ __device__ constexpr int al32(int x) { return (x + 31) & ~31; }
 struct FwdStage {
     int o_pp, o_S, o_sp, o_dc, o_dpp, o_vm, floats;
 };
+// pcs: the model S is per shot channel (shot-innermost like the wavefields)
 __host__ __device__ inline FwdStage fwd_stage(int TXV, int TY, bool is3d, bool born, int C, int logC,
-                                              bool has_sp) {
+                                              bool has_sp, bool pcs = false) {
     const int HF = C < 4 ? 4 : C;
     const int TXF = 4 * TXV;
     const int rows = TY + (is3d ? 2 : 0);
@@ -62,7 +63,7 @@ __host__ __device__ inline FwdStage fwd_stage(int TXV, int TY, bool is3d, bool b
     FwdStage s{};
     s.o_pp = al32(rows * SR);
     s.o_S = s.o_pp + al32(TY * TXF);
-    s.o_sp = s.o_S + al32(TY * cells);
+    s.o_sp = s.o_S + al32(TY * (pcs ? TXF : cells));
     int end = s.o_sp + (has_sp ? al32(TY * cells) : 0);
     s.o_dc = end;
     if (born) {
@@ -316,7 +317,10 @@ static __device__ __noinline__ InjStep inject_residuals(float4 lk4, const RxEnt*
 // ---------------------------------------------------------------------------
 // forward step, TMA ring
 // ---------------------------------------------------------------------------
-template <int TXV, int TY, bool IS3D, bool BORN, int C>
+// PCS: every shot channel has its own model (S in the wavefields' layout,
+// read as the own tile of a wavefield) -- the shots of co-admitted requests on
+// different models advancing in one launch; forward sweeps only, C >= 4.
+template <int TXV, int TY, bool IS3D, bool BORN, int C, bool PCS = false>
 __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : ((TXV * TY >= 256) ? 4 : 8)) k_forward_tma(const FwdArgs a, const __grid_constant__ FwdMaps mp,
                                                          const int R, int* err) {
     extern __shared__ __align__(128) float smf[];
@@ -329,7 +333,8 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
     constexpr int SR = TXF + 2 * HF;
     constexpr int cells = TXF >> logC;
     const bool has_sp = a.sp != nullptr;
-    const FwdStage L = fwd_stage(TXV, TY, IS3D, BORN, C, logC, has_sp);
+    static_assert(!PCS || (!BORN && C >= 4), "per-channel models: forward sweeps with C >= 4");
+    const FwdStage L = fwd_stage(TXV, TY, IS3D, BORN, C, logC, has_sp, PCS);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smf + (size_t)R * L.floats);
 
     const int tx = threadIdx.x;
@@ -367,7 +372,9 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         uint64_t* bar = bars + slot;
         const bool inner = i >= 1 && i <= nloc - 2;
         uint32_t bytes = b_halo * (BORN ? 2u : 1u);
-        if (inner) bytes += b_own * (BORN ? 2u : 1u) + b_cell * (1u + (has_sp ? 1u : 0u) + (BORN ? 1u : 0u));
+        if (inner)
+            bytes += b_own * (BORN ? 2u : 1u) + (PCS ? b_own : b_cell) +
+                     b_cell * ((has_sp ? 1u : 0u) + (BORN ? 1u : 0u));
         if (a.wait_test && i == 0) bytes += 16u;   // never delivered: exercises the bounded wait
         mbar_expect_tx(bar, bytes);
         if (C >= 4) tma4(st, &mp.pc, bar, 0, x0c - 1, y0 - HR, p);
@@ -379,7 +386,8 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         if (inner) {
             if (C >= 4) tma4(st + L.o_pp, &mp.pp, bar, 0, x0c, y0, p);
             else tma3(st + L.o_pp, &mp.pp, bar, fx0, y0, p);
-            tma3(st + L.o_S, &mp.S, bar, x0c, y0, p);
+            if (PCS) tma4(st + L.o_S, &mp.S, bar, 0, x0c, y0, p);
+            else tma3(st + L.o_S, &mp.S, bar, x0c, y0, p);
             if (has_sp) tma3(st + L.o_sp, &mp.sp, bar, x0c, y0, p);
             if (BORN) {
                 if (C >= 4) tma4(st + L.o_dpp, &mp.dpp, bar, 0, x0c, y0, p);
@@ -442,7 +450,8 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         const float4 cm = ld4(sm_m + r * SR + col);
         const float4 cp = ld4(sm_p + r * SR + col);
         const float4 ppv = ld4(sm_c + L.o_pp + ty * TXF + 4 * tx);
-        const float4 Sv = cell4s(sm_c + L.o_S + ty * cells, 4 * tx, logC);
+        const float4 Sv = PCS ? ld4(sm_c + L.o_S + ty * TXF + 4 * tx)
+                              : cell4s(sm_c + L.o_S + ty * cells, 4 * tx, logC);
         const float4 spv = has_sp ? cell4s(sm_c + L.o_sp + ty * cells, 4 * tx, logC) : f4zero();
         const bool zy_in = y_in && z >= 1 && z <= g.nz - 2;
         const bool all_in = zy_in && x_all;
@@ -733,7 +742,8 @@ struct TmaLaunch {
     bool is3d;
 };
 template <int C>
-int tma_forward(const TmaLaunch& t, const FwdArgs& a, const FwdMaps& mp, bool born);
+int tma_forward(const TmaLaunch& t, const FwdArgs& a, const FwdMaps& mp, bool born,
+                bool pcs = false);
 template <int C>
 int tma_adjoint(const TmaLaunch& t, const AdjArgs& a, const AdjMaps& mp);
 template <int C>

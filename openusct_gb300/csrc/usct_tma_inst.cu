@@ -15,8 +15,17 @@ namespace usct {
 
 namespace {
 template <int kC, int TX, int TY_, bool D3>
-int fwd_tile(const TmaLaunch& t, const FwdArgs& a, const FwdMaps& mp, bool born) {
+int fwd_tile(const TmaLaunch& t, const FwdArgs& a, const FwdMaps& mp, bool born, bool pcs) {
     if constexpr (tma_tile_ok(TX, kC, D3)) {
+        if (pcs) {
+            if constexpr (kC >= 4) {
+                k_forward_tma<TX, TY_, D3, false, kC, true>
+                    <<<t.grid, dim3(TX, TY_), t.smem, t.stream>>>(a, mp, t.R, t.err);
+                return 0;
+            } else {
+                return -1;
+            }
+        }
         if (born)
             k_forward_tma<TX, TY_, D3, true, kC>
                 <<<t.grid, dim3(TX, TY_), t.smem, t.stream>>>(a, mp, t.R, t.err);
@@ -68,6 +77,9 @@ void allow_tile(int bytes) {
                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         cudaFuncSetAttribute(k_forward_tma<TX, TY_, D3, true, kC>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if constexpr (kC >= 4)
+            cudaFuncSetAttribute(k_forward_tma<TX, TY_, D3, false, kC, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         cudaFuncSetAttribute(k_adjoint_tma<TX, TY_, D3, kC>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     }
@@ -76,20 +88,20 @@ void allow_tile(int bytes) {
 
 // the tiles: 3D 32x4, 32x8, 64x2, 64x4; 2D 64x1, 128x1 (key = tile_x * 1000 + tile_y)
 template <int kC>
-int tma_forward(const TmaLaunch& t, const FwdArgs& a, const FwdMaps& mp, bool born) {
+int tma_forward(const TmaLaunch& t, const FwdArgs& a, const FwdMaps& mp, bool born, bool pcs) {
     const int key = t.txv * 1000 + t.ty;
     if (t.is3d) {
         switch (key) {
-            case 32004: return fwd_tile<kC, 32, 4, true>(t, a, mp, born);
-            case 32008: return fwd_tile<kC, 32, 8, true>(t, a, mp, born);
-            case 64002: return fwd_tile<kC, 64, 2, true>(t, a, mp, born);
-            case 64004: return fwd_tile<kC, 64, 4, true>(t, a, mp, born);
+            case 32004: return fwd_tile<kC, 32, 4, true>(t, a, mp, born, pcs);
+            case 32008: return fwd_tile<kC, 32, 8, true>(t, a, mp, born, pcs);
+            case 64002: return fwd_tile<kC, 64, 2, true>(t, a, mp, born, pcs);
+            case 64004: return fwd_tile<kC, 64, 4, true>(t, a, mp, born, pcs);
             default: return -1;
         }
     }
     switch (key) {
-        case 64001: return fwd_tile<kC, 64, 1, false>(t, a, mp, born);
-        case 128001: return fwd_tile<kC, 128, 1, false>(t, a, mp, born);
+        case 64001: return fwd_tile<kC, 64, 1, false>(t, a, mp, born, pcs);
+        case 128001: return fwd_tile<kC, 128, 1, false>(t, a, mp, born, pcs);
         default: return -1;
     }
 }
@@ -141,7 +153,7 @@ void tma_allow_smem(int bytes) {
     allow_tile<kC, 128, 1, false>(bytes);
 }
 
-template int tma_forward<USCT_TMA_C>(const TmaLaunch&, const FwdArgs&, const FwdMaps&, bool);
+template int tma_forward<USCT_TMA_C>(const TmaLaunch&, const FwdArgs&, const FwdMaps&, bool, bool);
 template int tma_adjoint<USCT_TMA_C>(const TmaLaunch&, const AdjArgs&, const AdjMaps&);
 template void tma_allow_smem<USCT_TMA_C>(int);
 template int tma_forward2<USCT_TMA_C>(const TmaLaunch2&, const Fwd2Args&, const Fwd2Maps&);

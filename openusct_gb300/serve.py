@@ -18,6 +18,13 @@ model, the observed data and every wavefield stay on the device across its
 iterations, and only scalars (misfits, CG dot products) reach the host until
 the final model.
 
+Forward requests that share grid, spacing, time axis and wavelet (and have
+no sponge or footprints) are put in one launch when a batch would otherwise
+be partly filled: when one is admitted, compatible requests already waiting
+join it up to a full batch of shots, and the group runs on one plan whose
+shot channels each carry their own model (``usct_plan_set_channel_models``).
+Every request of a group gets exactly the traces it would get alone.
+
 Latency is measured from a request's arrival to its result being on the host;
 ``Stats`` gives p50/p99 and shots/s.  The scheduling logic is independent of
 the executor (``GpuExecutor`` here), so it is tested on the CPU with a fake.
@@ -91,6 +98,7 @@ class Result:
     t_admit: float = 0.0
     t_done: float = 0.0
     waited_for_budget: bool = False      # a slot was free but its footprint did not fit
+    group: int = 1                       # requests that shared its launches
 
     @property
     def latency(self):
@@ -102,7 +110,7 @@ class Result:
                 "shots": self.shots, "device_bytes": self.footprint,
                 "t_arrival": self.t_arrival, "t_admit": self.t_admit, "t_done": self.t_done,
                 "queue_s": max(0.0, self.t_admit - self.t_arrival),
-                "waited_for_budget": self.waited_for_budget,
+                "waited_for_budget": self.waited_for_budget, "group": self.group,
                 "latency_s": self.latency if self.ok else None}
 
 
@@ -120,6 +128,7 @@ class Stats:
     max_concurrent: int
     peak_reserved_bytes: int
     waited_for_budget: int = 0
+    merged: int = 0                      # requests served in a shared launch group
 
     def as_dict(self):
         return dict(self.__dict__)
@@ -189,8 +198,20 @@ class _PlanBackend:
         return hv
 
 
+def _concat_csr(parts):
+    """Rows of several element CSR lists, one after the other."""
+    from .geometry import CSR
+    ptr = [0]
+    for c in parts:
+        ptr.extend(int(v) + ptr[-1] for v in c.ptr[1:])
+    return CSR(np.asarray(ptr, np.int32), np.concatenate([c.cell for c in parts]),
+               np.concatenate([c.w for c in parts]))
+
+
 class GpuExecutor:
     """Runs one request on the GB300 engine on its own stream."""
+
+    merge_width = 32   # shots of one launch group (a batch)
 
     def __init__(self, device=None, graphs=False, workspace_bytes=None):
         import torch
@@ -289,6 +310,75 @@ class GpuExecutor:
             plan.check(st)
             return {"J": float(J.sum().item()), "g": g.cpu().numpy()}
 
+    # -- forward requests sharing launches --------------------------------------
+    def merge_key(self, req):
+        """Requests with equal keys can share a plan with per-channel models:
+        forward requests of the same grid, spacing, time axis and wavelet,
+        without sponge or footprints; None for any other request."""
+        if req.kind != "forward" or req.sponge is not None or req.footprints is not None \
+                or req.batch is not None:
+            return None
+        w = np.ascontiguousarray(req.wavelet, np.float64)[: req.nt]
+        return (tuple(np.shape(req.m)), float(req.h), float(req.dt), int(req.nt), w.tobytes())
+
+    def plan_for_group(self, reqs):
+        """One plan for the transmits of all ``reqs`` (in order) and the union of
+        their receivers; transmit t uses the model of the request it came from."""
+        from .backend import Plan
+        from .geometry import element_csr
+        shape = tuple(np.shape(reqs[0].m))
+        parts = [element_csr(q.geom, shape, q.src_list, None) for q in reqs]
+        tx = _concat_csr([t for t, _ in parts])
+        rx = _concat_csr([r for _, r in parts])
+        C = self.merge_width
+        q0 = reqs[0]
+        plan = Plan(shape, q0.h, q0.dt, q0.nt, tx, rx, batch=C)
+        owner = np.concatenate([np.full(t.rows, i, np.int32) for i, (t, _) in enumerate(parts)])
+        _lib.check(plan._lib.usct_plan_set_channel_models(
+            plan.handle, len(reqs), owner.ctypes.data_as(_lib._ip)))
+        if not self.graphs:
+            plan.set("graphs", 0)
+        plan.group_parts = [(t.rows, r.rows) for t, r in parts]
+        return plan
+
+    def footprint_group(self, reqs, plan):
+        data = 4 * plan.n_tx * plan.nt * plan.n_rx
+        cells = int(np.prod(plan.shape))
+        return (plan.model_bytes() + plan.batch_bytes(_lib.MODE_FORWARD) + data +
+                8 * len(reqs) * cells + (1 << 20))
+
+    def run_group(self, reqs, plan):
+        """The forward sweeps of every request of the group in shared launches;
+        returns each request's traces (its transmits x its receivers)."""
+        torch = self.torch
+        from .backend import _ptr, _stream, _wavelet
+        lib = plan._lib
+        dev = self.device
+        st = torch.cuda.Stream(device=dev)
+        with torch.cuda.stream(st):
+            models = torch.stack([torch.from_numpy(np.ascontiguousarray(q.m, np.float64))
+                                  for q in reqs]).to(dev)
+            w = _wavelet(reqs[0].wavelet, reqs[0].nt, dev)
+            mws = torch.empty(plan.model_bytes(), dtype=torch.uint8, device=dev)
+            bws = torch.empty(plan.batch_bytes(_lib.MODE_FORWARD), dtype=torch.uint8, device=dev)
+            data = torch.empty((plan.n_tx, plan.nt, plan.n_rx), dtype=torch.float32, device=dev)
+            s = _stream(st)
+            _lib.check(lib.usct_model_prepare_channels(plan.handle, _ptr(mws), _ptr(models),
+                                                       _ptr(w), s))
+            for b in range(plan.nbatch):
+                if any(q.cancelled.is_set() for q in reqs):
+                    raise Cancelled(f"cancelled after {b} of {plan.nbatch} shot batches")
+                _lib.check(lib.usct_batch_forward(plan.handle, _ptr(mws), _ptr(bws), b,
+                                                  _lib.MODE_FORWARD, _ptr(data), s))
+            plan.check(st)
+            host = data.cpu().numpy()
+        out, t0, r0 = [], 0, 0
+        for nt_i, nr_i in plan.group_parts:
+            out.append({"traces": np.ascontiguousarray(host[t0:t0 + nt_i, :, r0:r0 + nr_i])})
+            t0 += nt_i
+            r0 += nr_i
+        return out
+
     def _gauss_newton(self, req, plan, m, w, sp, mws, st):
         """``n_iter`` Gauss-Newton iterations of the device-resident invert on
         this request's plan; cancellation is checked between iterations."""
@@ -357,6 +447,56 @@ class Engine:
                 self.lock.notify_all()
             on_done(res)
 
+    def _worker_group(self, members, plan, fp, t0, on_done):
+        """Requests sharing one plan with per-channel models."""
+        reqs = [m[1] for m in members]
+        results = [m[2] for m in members]
+        try:
+            outs = self.ex.run_group(reqs, plan)
+            for res, out in zip(results, outs):
+                res.ok = True
+                res.traces = out.get("traces")
+        except Exception as exc:
+            for res in results:
+                res.ok = False
+                res.error = f"{type(exc).__name__}: {exc}"[:300]
+        finally:
+            try:
+                self.ex.release(plan)
+            except Exception:
+                pass
+            t = time.perf_counter() - t0
+            for res in results:
+                res.t_done = t
+                res.group = len(members)
+            with self.lock:
+                self.reserved -= fp
+                self.active -= 1
+                self.lock.notify_all()
+            for res in results:
+                on_done(res)
+
+    def _group_for(self, head, others, results):
+        """Waiting requests that can share ``head``'s launches (same merge key,
+        shots up to one batch), as (index, request) pairs starting with head;
+        None when there are none."""
+        key_of = getattr(self.ex, "merge_key", None)
+        if key_of is None:
+            return None
+        i, rq = head
+        width = getattr(self.ex, "merge_width", 32)
+        key = key_of(rq)
+        if key is None or rq.n_shots >= width:
+            return None
+        group, shots = [head], rq.n_shots
+        for item in sorted(others, key=lambda it: (it[0], it[1])):
+            j, oq = item[1], item[2]
+            if oq.cancelled.is_set() or shots + oq.n_shots > width or key_of(oq) != key:
+                continue
+            group.append((j, oq))
+            shots += oq.n_shots
+        return group if len(group) > 1 else None
+
     # -- a whole stream ----------------------------------------------------------
     def run_stream(self, requests, realtime=True):
         """Replay ``requests`` (sorted by arrival) and return their Results in
@@ -418,6 +558,44 @@ class Engine:
                         self.ex.release(plan)
                         done_count[0] += 1
                         continue
+                    group = None
+                    if self.active < self.max_active:
+                        group = self._group_for((i, rq), pending + keep, results)
+                    if group:
+                        gplan, gfp = None, 0
+                        try:
+                            gplan = self.ex.plan_for_group([q for _, q in group])
+                            gfp = int(self.ex.footprint_group([q for _, q in group], gplan))
+                        except Exception:
+                            if gplan is not None:
+                                self.ex.release(gplan)
+                            gplan = None
+                        if gplan is not None and self.reserved + gfp <= self.budget:
+                            taken = {j for j, _ in group}
+                            for it in pending + keep:
+                                if it[1] in taken:
+                                    self.ex.release(it[3])
+                            self.ex.release(plan)
+                            pending[:] = [it for it in pending if it[1] not in taken]
+                            heapq.heapify(pending)
+                            keep = [it for it in keep if it[1] not in taken]
+                            self.reserved += gfp
+                            self.active += 1
+                            self.peak_reserved = max(self.peak_reserved, self.reserved)
+                            self.max_concurrent = max(self.max_concurrent, self.active)
+                            now_a = time.perf_counter() - t0
+                            members = []
+                            for j, q in group:
+                                results[j].t_admit = now_a
+                                members.append((j, q, results[j]))
+                            th = threading.Thread(target=self._worker_group,
+                                                  args=(members, gplan, gfp, t0, on_done),
+                                                  daemon=True)
+                            threads.append(th)
+                            th.start()
+                            continue
+                        if gplan is not None:
+                            self.ex.release(gplan)
                     if self.active < self.max_active and self.reserved + fp <= self.budget:
                         self.reserved += fp
                         self.active += 1
@@ -469,7 +647,8 @@ def summarize(results, engine=None):
                  shots=shots, shots_per_s=shots / span,
                  max_concurrent=engine.max_concurrent if engine else 0,
                  peak_reserved_bytes=engine.peak_reserved if engine else 0,
-                 waited_for_budget=sum(1 for r in results if r.waited_for_budget))
+                 waited_for_budget=sum(1 for r in results if r.waited_for_budget),
+                 merged=sum(1 for r in results if r.ok and r.group > 1))
 
 
 # ---------------------------------------------------------------------------

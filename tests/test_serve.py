@@ -185,3 +185,55 @@ def test_per_request_records(tmp_path):
     assert not recs[1]["ok"] and recs[1]["error"].startswith("rejected")
     assert recs[1]["latency_s"] is None
     assert all(r["queue_s"] >= 0 for r in recs)
+
+
+class MergingExecutor(FakeExecutor):
+    """Forward requests tagged alike (``m[3]``) may share launches."""
+
+    merge_width = 32
+
+    def __init__(self):
+        super().__init__()
+        self.groups = []
+
+    def merge_key(self, req):
+        return req.m[3] if req.kind == "forward" and len(req.m) > 3 else None
+
+    def plan_for(self, req):
+        fp, dur, fail = req.m[:3]
+        return FakePlan(int(fp), float(dur), bool(fail))
+
+    def plan_for_group(self, reqs):
+        return FakePlan(sum(int(q.m[0]) for q in reqs), max(float(q.m[1]) for q in reqs))
+
+    def footprint_group(self, reqs, plan):
+        return plan.fp
+
+    def run_group(self, reqs, plan):
+        self.groups.append([q.rid for q in reqs])
+        time.sleep(plan.dur)
+        return [{"traces": np.full(2, q.rid)} for q in reqs]
+
+
+def fwd(fp, dur, arrival, tag, shots=2):
+    r = Request(kind="forward", m=(fp, dur, False, tag),
+                geom=type("G", (), {"idx": list(range(shots))})(), wavelet=None, dt=1.0, h=1.0,
+                nt=2, arrival=arrival)
+    return r
+
+
+def test_waiting_compatible_forward_requests_share_one_launch_group():
+    """While a long request holds the only slot, three compatible forward
+    requests and one of another grid queue; when the slot frees, the first
+    admitted takes the other two compatible ones into its group (up to one
+    batch of shots), each gets its own result, and the other grid runs alone."""
+    ex = MergingExecutor()
+    eng = Engine(ex, budget_bytes=1000, max_active=1)
+    rs = eng.run_stream([req(10, 0.2, 0.0), fwd(10, 0.02, 0.01, "a"), fwd(10, 0.02, 0.02, "a"),
+                         fwd(10, 0.02, 0.03, "b"), fwd(10, 0.02, 0.04, "a", shots=40)])
+    assert all(r.ok for r in rs)
+    assert ex.groups == [[1, 2]]
+    assert rs[1].group == 2 and rs[2].group == 2 and rs[3].group == 1 and rs[4].group == 1
+    assert list(rs[1].traces) == [1, 1] and list(rs[2].traces) == [2, 2]
+    assert summarize(rs, eng).merged == 2
+    assert eng.reserved == 0 and eng.active == 0
