@@ -203,7 +203,8 @@ def _concat_csr(parts):
     from .geometry import CSR
     ptr = [0]
     for c in parts:
-        ptr.extend(int(v) + ptr[-1] for v in c.ptr[1:])
+        base = ptr[-1]
+        ptr.extend(int(v) + base for v in c.ptr[1:])
     return CSR(np.asarray(ptr, np.int32), np.concatenate([c.cell for c in parts]),
                np.concatenate([c.w for c in parts]))
 

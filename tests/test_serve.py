@@ -237,3 +237,14 @@ def test_waiting_compatible_forward_requests_share_one_launch_group():
     assert list(rs[1].traces) == [1, 1] and list(rs[2].traces) == [2, 2]
     assert summarize(rs, eng).merged == 2
     assert eng.reserved == 0 and eng.active == 0
+
+
+def test_concatenated_element_lists():
+    from openusct_gb300.geometry import element_csr
+    from openusct_gb300.serve import _concat_csr
+    a = element_csr([(1, 2), (3, 4), (5, 6)], (8, 8), [0, 2])
+    b = element_csr([(7, 7), (0, 1)], (8, 8), [1])
+    tx = _concat_csr([a[0], b[0]])
+    rx = _concat_csr([a[1], b[1]])
+    assert list(tx.ptr) == [0, 1, 2, 3] and list(tx.cell) == [1 * 8 + 2, 5 * 8 + 6, 0 * 8 + 1]
+    assert list(rx.ptr) == [0, 1, 2, 3, 4, 5] and rx.rows == 5 and len(rx.w) == 5
