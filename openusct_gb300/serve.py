@@ -214,9 +214,10 @@ class GpuExecutor:
 
     merge_width = 32   # shots of one launch group (a batch)
 
-    def __init__(self, device=None, graphs=False, workspace_bytes=None):
+    def __init__(self, device=None, graphs=False, workspace_bytes=None, merge=True):
         import torch
         self.torch = torch
+        self.merge = merge   # compatible forward requests may share launches
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.graphs = graphs
         # the batch workspace one request may size its checkpoint interval for
@@ -316,8 +317,8 @@ class GpuExecutor:
         """Requests with equal keys can share a plan with per-channel models:
         forward requests of the same grid, spacing, time axis and wavelet,
         without sponge or footprints; None for any other request."""
-        if req.kind != "forward" or req.sponge is not None or req.footprints is not None \
-                or req.batch is not None:
+        if not self.merge or req.kind != "forward" or req.sponge is not None \
+                or req.footprints is not None or req.batch is not None:
             return None
         w = np.ascontiguousarray(req.wavelet, np.float64)[: req.nt]
         return (tuple(np.shape(req.m)), float(req.h), float(req.dt), int(req.nt), w.tobytes())
