@@ -339,17 +339,18 @@ def gauss_newton_phase(args):
 
 
 def co_admission():
-    """Compatible small forward requests (16 requests of 8 shots on one 2D
-    256^2 grid, each on its own model, arriving together) served with shared
-    launches (per-channel models, up to 32 shots a launch) and with one plan
-    per request; shots/s both ways, and that the traces agree."""
+    """Compatible small forward requests (48 requests of 8 shots on one 2D
+    256^2 grid, each on its own model, arriving together: more than the 12
+    slots) served with shared launches (per-channel models, up to 32 shots a
+    launch) and with one plan per request; shots/s both ways, and that the
+    traces agree."""
     import numpy as np
     from openusct_gb300 import problems
     from openusct_gb300.serve import Engine, GpuExecutor, Request, summarize
     base = problems.ring2d(seed=0)
     rng = np.random.default_rng(5)
     reqs = []
-    for k in range(16):
+    for k in range(48):
         m = base.m_true * (1.0 + 0.005 * rng.standard_normal(base.m_true.shape))
         src = [int(s) for s in rng.choice(len(base.geom.idx), size=8, replace=False)]
         reqs.append(Request(kind="forward", m=m, geom=base.geom, wavelet=base.wavelet,
@@ -367,7 +368,7 @@ def co_admission():
         traces[name] = [r.traces for r in res]
     out["traces_equal"] = all(np.array_equal(a, b) for a, b in zip(traces["shared"],
                                                                    traces["separate"]))
-    out["stream"] = ("16 forward requests of 8 shots, 2D 256^2 ring (64 elements), nt=1500, each "
+    out["stream"] = ("48 forward requests of 8 shots, 2D 256^2 ring (64 elements), nt=1500, each "
                      "on its own perturbed model, arriving together; 12 slots")
     return out
 

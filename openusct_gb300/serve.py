@@ -479,9 +479,12 @@ class Engine:
                 on_done(res)
 
     def _group_for(self, head, others, results):
-        """Waiting requests that can share ``head``'s launches (same merge key,
-        shots up to one batch), as (index, request) pairs starting with head;
-        None when there are none."""
+        """Waiting requests that share ``head``'s launches, as (index, request)
+        pairs starting with head; None for none.  Separate plans on their own
+        streams already overlap on the device, and a shared launch reads the
+        model once per shot, so requests are grouped only when more compatible
+        ones wait than there are free slots: ceil(waiting / free) requests per
+        group, in arrival order, their shots up to one batch."""
         key_of = getattr(self.ex, "merge_key", None)
         if key_of is None:
             return None
@@ -490,10 +493,18 @@ class Engine:
         key = key_of(rq)
         if key is None or rq.n_shots >= width:
             return None
+        cands = [it for it in sorted(others, key=lambda it: (it[0], it[1]))
+                 if not it[2].cancelled.is_set() and key_of(it[2]) == key]
+        free = max(1, self.max_active - self.active)
+        size = -(-(len(cands) + 1) // free)
+        if size < 2:
+            return None
         group, shots = [head], rq.n_shots
-        for item in sorted(others, key=lambda it: (it[0], it[1])):
+        for item in cands:
+            if len(group) == size:
+                break
             j, oq = item[1], item[2]
-            if oq.cancelled.is_set() or shots + oq.n_shots > width or key_of(oq) != key:
+            if shots + oq.n_shots > width:
                 continue
             group.append((j, oq))
             shots += oq.n_shots

@@ -225,8 +225,8 @@ def fwd(fp, dur, arrival, tag, shots=2):
 def test_waiting_compatible_forward_requests_share_one_launch_group():
     """While a long request holds the only slot, three compatible forward
     requests and one of another grid queue; when the slot frees, the first
-    admitted takes the other two compatible ones into its group (up to one
-    batch of shots), each gets its own result, and the other grid runs alone."""
+    admitted takes the other compatible one that fits one batch of shots into
+    its group, each gets its own result, and the other grid runs alone."""
     ex = MergingExecutor()
     eng = Engine(ex, budget_bytes=1000, max_active=1)
     rs = eng.run_stream([req(10, 0.2, 0.0), fwd(10, 0.02, 0.01, "a"), fwd(10, 0.02, 0.02, "a"),
@@ -248,3 +248,18 @@ def test_concatenated_element_lists():
     rx = _concat_csr([a[1], b[1]])
     assert list(tx.ptr) == [0, 1, 2, 3] and list(tx.cell) == [1 * 8 + 2, 5 * 8 + 6, 0 * 8 + 1]
     assert list(rx.ptr) == [0, 1, 2, 3, 4, 5] and rx.rows == 5 and len(rx.w) == 5
+
+
+def test_requests_are_grouped_only_when_they_outnumber_the_free_slots():
+    ex = MergingExecutor()
+    eng = Engine(ex, budget_bytes=10 ** 6, max_active=4)
+    rs = eng.run_stream([fwd(10, 0.05, 0.0, "a") for _ in range(3)], realtime=False)
+    assert all(r.ok and r.group == 1 for r in rs) and ex.groups == []
+    ex = MergingExecutor()
+    eng = Engine(ex, budget_bytes=10 ** 6, max_active=4)
+    rs = eng.run_stream([fwd(10, 0.05, 0.0, "a") for _ in range(10)], realtime=False)
+    assert all(r.ok for r in rs)
+    # 10 waiting for 4 slots: groups of ceil(10/4) = 3, then ceil(7/3) = 3,
+    # ceil(4/2) = 2 and ceil(2/1) = 2 -- every request admitted at once
+    assert sorted(len(g) for g in ex.groups) == [2, 2, 3, 3]
+    assert eng.max_concurrent == 4
