@@ -18,12 +18,13 @@ model, the observed data and every wavefield stay on the device across its
 iterations, and only scalars (misfits, CG dot products) reach the host until
 the final model.
 
-Forward requests that share grid, spacing, time axis and wavelet (and have
-no sponge or footprints) are put in one launch when a batch would otherwise
-be partly filled: when one is admitted, compatible requests already waiting
-join it up to a full batch of shots, and the group runs on one plan whose
-shot channels each carry their own model (``usct_plan_set_channel_models``).
-Every request of a group gets exactly the traces it would get alone.
+With ``GpuExecutor(merge=True)``, forward requests that share grid, spacing,
+time axis and wavelet (and have no sponge or footprints) are put in shared
+launches when more of them wait than there are free slots: when one is
+admitted, compatible requests already waiting join it (up to a batch of
+shots), and the group runs on one plan whose shot channels each carry their
+own model (``usct_plan_set_channel_models``).  Every request of a group gets
+exactly the traces it would get alone.
 
 Latency is measured from a request's arrival to its result being on the host;
 ``Stats`` gives p50/p99 and shots/s.  The scheduling logic is independent of
@@ -214,10 +215,12 @@ class GpuExecutor:
 
     merge_width = 32   # shots of one launch group (a batch)
 
-    def __init__(self, device=None, graphs=False, workspace_bytes=None, merge=True):
+    def __init__(self, device=None, graphs=False, workspace_bytes=None, merge=False):
         import torch
         self.torch = torch
-        self.merge = merge   # compatible forward requests may share launches
+        # compatible forward requests may share launches (measured slower than
+        # separate plans on concurrent streams on 2D streams, so off by default)
+        self.merge = merge
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.graphs = graphs
         # the batch workspace one request may size its checkpoint interval for

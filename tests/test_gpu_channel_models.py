@@ -123,7 +123,7 @@ def test_served_forward_requests_share_launches_and_match_alone(eng):
         c[(yy - cy) ** 2 + (xx - cx) ** 2 <= 64] = 1580.0
         reqs.append(Request(kind="forward", m=1.0 / c ** 2, geom=ring, wavelet=wav, dt=dt, h=h,
                             nt=nt, src_list=list(range(k, k + 5)), arrival=0.001 * k))
-    ex = GpuExecutor()
+    ex = GpuExecutor(merge=True)
     mixed = Engine(ex, budget_bytes=20 << 30, max_active=1).run_stream(reqs, realtime=False)
     assert all(r.ok for r in mixed), [r.error for r in mixed]
     assert max(r.group for r in mixed) > 1
