@@ -907,7 +907,6 @@ static int launch_adj_tma(usct_plan* p, const AdjArgs& a0, cudaStream_t s) {
     TRY(get_map(p, a.d2, MK_WF_OWN, &mp.d2));
     if (a.sp) TRY(get_map(p, a.sp, MK_CELL_OWN, &mp.sp));
     if (a.gacc) TRY(get_map(p, a.gacc, MK_G_OWN, &mp.g));
-    TRY(get_map(p, a.lk, MK_WF_OWN, &mp.lk));   // lam^k leaves by tensor stores
     const int R = p->stages_adj;
     const AdjStage L = adj_stage(p->txv, p->ty, p->ndim == 3, p->C, p->logC, a.sp != nullptr,
                                  a.gacc != nullptr);

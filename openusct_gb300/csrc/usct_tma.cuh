@@ -43,7 +43,7 @@ struct FwdMaps {
     CUtensorMap pc, pp, S, sp, dc, dpp, vm;
 };
 struct AdjMaps {
-    CUtensorMap l1, S, l2, d2, sp, g, lk;
+    CUtensorMap l1, S, l2, d2, sp, g;
 };
 
 __host__ __device__ constexpr int al32(int x) { return (x + 31) & ~31; }
@@ -170,31 +170,6 @@ __device__ __forceinline__ void tma4(void* dst, const CUtensorMap* map, uint64_t
         "r"(c3)
         : "memory");
 }
-
-// tensor stores from shared memory (bulk groups): the box at the coordinates
-// is written from the shared tile; parts outside the tensor are clipped
-__device__ __forceinline__ void tma_store4(const CUtensorMap* map, const void* src, int c0, int c1,
-                                           int c2, int c3) {
-    asm volatile(
-        "cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(
-            reinterpret_cast<uint64_t>(map)),
-        "r"(smem_u32(src)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
-        : "memory");
-}
-__device__ __forceinline__ void tma_store3(const CUtensorMap* map, const void* src, int c0, int c1,
-                                           int c2) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
-            reinterpret_cast<uint64_t>(map)),
-        "r"(smem_u32(src)), "r"(c0), "r"(c1), "r"(c2)
-        : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-// the committed stores have read their shared tiles / have completed
-__device__ __forceinline__ void bulk_wait_read_all() {
-    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-}
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // cell-layout row (smem) expanded to the 4 floats starting at float lf
 __device__ __forceinline__ float4 cell4s(const float* row, int lf, int logC) {
@@ -588,6 +563,7 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
     const int y = y0 + ty;
     const bool own = (f < g.RP) && (y < g.ny);
     const int r = ty + HR;
+    const long long ro = (long long)y * g.RP + f;
     const bool y_in = !IS3D || (y >= 1 && y <= g.ny - 2);
     bool x_in[4];
 #pragma unroll
@@ -656,6 +632,8 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
     uint32_t ph_p = (R == 2) ? 1u : 0u;
     bool ok = wait_bar(bars + 0, 0u);
     ok = wait_bar(bars + 1, 0u) && ok;
+    float* lk_ptr = a.lk + (long long)z0 * g.PP + ro;
+    double* g_row = has_g ? a.gacc + (long long)z0 * g.CPP + (long long)y * g.nxs + x0c : nullptr;
     for (int z = z0; z < z1; ++z) {
         const int im = z - z0;
         ok = wait_bar(bars + s_p, ph_p) && ok;
@@ -703,27 +681,25 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
             ri = st.ri;
             rnz = st.rnz;
         }
-        // lam^k and the updated gradient go back into this plane's stage, over
-        // lam^{k+2} and the loaded gradient (each thread overwrites what only
-        // it read), and leave by tensor stores of the own tile; cells outside
-        // the grid are clipped by the stores as they were skipped by `own`
-        float* sw = const_cast<float*>(sm_c);
-        st4(sw + L.o_l2 + ty * TXF + lf, make_float4(lk[0], lk[1], lk[2], lk[3]));
+        if (own) st4(lk_ptr, make_float4(lk[0], lk[1], lk[2], lk[3]));
+        lk_ptr += g.PP;
         if (has_g) {
             float pr[4];
             put4(pr, own ? mul4(make_float4(lk[0], lk[1], lk[2], lk[3]), d2v) : f4zero());
-            double* gs = reinterpret_cast<double*>(sw + L.o_g) + ty * cells;
+            const double* gs = reinterpret_cast<const double*>(sm_c + L.o_g) + ty * cells;
+            double* grow = g_row;
+            g_row += g.CPP;
             if (logC == 0) {
                 if (own) {
                     const int c0 = lf;
-                    double2* gp = reinterpret_cast<double2*>(gs + c0);
+                    double2* gp = reinterpret_cast<double2*>(grow + c0);
                     gp[0] = make_double2(gs[c0] + (double)pr[0], gs[c0 + 1] + (double)pr[1]);
                     gp[1] = make_double2(gs[c0 + 2] + (double)pr[2], gs[c0 + 3] + (double)pr[3]);
                 }
             } else if (logC == 1) {
                 if (own) {
                     const int c0 = lf >> 1;
-                    *reinterpret_cast<double2*>(gs + c0) =
+                    *reinterpret_cast<double2*>(grow + c0) =
                         make_double2(gs[c0] + (double)(pr[0] + pr[1]), gs[c0 + 1] + (double)(pr[2] + pr[3]));
                 }
             } else {
@@ -731,21 +707,15 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
                 const int G = C >> 2;
                 for (int o = 1; o < G; o <<= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
                 const int c0 = lf >> logC;
-                if (own && (tx & (G - 1)) == 0) gs[c0] = gs[c0] + (double)s;
+                if (own && (tx & (G - 1)) == 0) grow[c0] = gs[c0] + (double)s;
             }
         }
-        fence_proxy_async();   // the staged tiles are visible to the tensor stores
 
         ok = __syncthreads_and(ok) != 0;
         if (!ok) break;
-        if (tid == 0) {
-            // the stores of plane z-1 read the stage about to be refilled
-            bulk_wait_read_all();
-            if (im + R < nloc) issue(im + R, s_m);
-            if (C >= 4) tma_store4(&mp.lk, sw + L.o_l2, 0, x0c, y0, z);
-            else tma_store3(&mp.lk, sw + L.o_l2, fx0, y0, z);
-            if (has_g) tma_store3(&mp.g, sw + L.o_g, x0c, y0, z);
-            bulk_commit();
+        if (tid == 0 && im + R < nloc) {
+            fence_proxy_async();
+            issue(im + R, s_m);
         }
         if (im + R < nloc) issued = im + R + 1;
         s_m = s_c;
@@ -756,8 +726,6 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
         if (tid == 0) atomicExch(err, 1);
         for (int i = (issued > R ? issued - R : 0); i < issued; ++i) (void)wait_stage(bars, i, R);
     }
-    // the tensor stores read shared memory: complete them before the CTA ends
-    if (tid == 0) bulk_wait_all();
 }
 
 // ---------------------------------------------------------------------------
