@@ -273,15 +273,22 @@ class GpuExecutor:
             sp = _grid_array(req.sponge, np.shape(req.m), "sponge", dev)
             mws = torch.empty(plan.model_bytes(), dtype=torch.uint8, device=dev)
             s = _stream(st)
-            # one shot batch at a time, the request's cancellation checked in
-            # between (the same calls, in the same order, as the whole-acquisition
-            # entry points, so results are identical)
+            # shot batches in order, one queued on the device behind the one
+            # running (so the device never waits for the host to enqueue the
+            # next), the request's cancellation checked between them; the same
+            # calls in the same order as the whole-acquisition entry points, so
+            # results are identical
             def batches():
+                prev = None
                 for b in range(plan.nbatch):
                     if req.cancelled.is_set():
                         raise Cancelled(f"cancelled after {b} of {plan.nbatch} shot batches")
                     yield b
-                    st.synchronize()
+                    ev = torch.cuda.Event()
+                    ev.record(st)
+                    if prev is not None:
+                        prev.synchronize()
+                    prev = ev
 
             if req.kind == "gauss-newton":
                 return self._gauss_newton(req, plan, m, w, sp, mws, st)
