@@ -343,8 +343,8 @@ def gauss_newton_phase(args):
 def latency_stream(dobs_fn, n=200):
     """Latency percentiles over a longer stream: 200 seeded requests at 20
     req/s (the serving configuration's mix and rate) with sizes scaled to
-    128^2-512^2 / 64^3-128^3 and 32-128 elements, so the service keeps up and
-    p99 is a percentile rather than the slowest request."""
+    128^2-512^2 / 64^3-128^3 and 32-128 elements, so that p99 is a percentile
+    rather than the slowest request (the 24-request stream's p99 is)."""
     from openusct_gb300.serve import Engine, GpuExecutor, make_stream, summarize
     reqs = make_stream(n, rate_hz=20.0, seed=12, sizes_2d=(128, 512), sizes_3d=(64, 128),
                        elements_2d=(32, 128), elements_3d=(64, 128), frac_gradient=0.3,
