@@ -379,3 +379,34 @@ def test_plan_cache_builds_plans_without_deadlock(monkeypatch):
     assert not th.is_alive(), "get_plan deadlocked"
     assert isinstance(out[0], StandIn) and out[0] in gb._LIVE_PLANS
     assert gb._held_workspace_bytes() >= 0
+
+
+def test_cpu_arm_memory_plan():
+    """The CPU arms keep the reference core's full-history plan (k = 0) when
+    the FP64 history fits 65 % of the host's available memory, else the
+    longest checkpoint interval whose checkpoints and segment fit; the
+    Gauss-Newton restatement always checkpoints."""
+    import importlib.util
+    import os
+    import types
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("bench_mod2", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    prob = types.SimpleNamespace(shape=(192, 192, 192), nt=2000)
+    N = 192 ** 3
+    hist = 2000 * N * 8
+    bench.host_available_bytes = lambda: 197 << 30
+    assert bench.cpu_shot_interval(prob, "grad") == (0, hist)
+    bench.host_available_bytes = lambda: 100 << 30
+    k, need = bench.cpu_shot_interval(prob, "grad")
+    assert 2 <= k < 1999 and need <= 0.65 * (100 << 30)
+    nseg = (1999 + k - 1) // k
+    assert need == (2 * nseg + k + 2) * N * 8
+    # the next longer interval would not fit
+    k2 = k + 1
+    nseg2 = (1999 + k2 - 1) // k2
+    assert (2 * nseg2 + k2 + 2) * N * 8 > 0.65 * (100 << 30)
+    bench.host_available_bytes = lambda: 197 << 30
+    kg, _ = bench.cpu_shot_interval(prob, "gn")
+    assert kg > 0
