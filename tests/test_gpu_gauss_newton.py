@@ -78,3 +78,18 @@ def test_gauss_newton_224_grid_vs_fp64(gb):
     hv = gb.gn_hessian_vector(p.m0, *args, src_list=sl)
     assert np.abs(ref).max() > 0.0
     assert rel_l2(hv, ref) < 1e-4
+
+
+@pytest.mark.slow
+def test_gauss_newton_224_full_time_axis_vs_fp64(gb):
+    """The Gauss-Newton configuration's full time axis (224^3, nt = 2500), one
+    seeded shot: Hv and the Born traces against the FP64 oracle (rel. L2
+    1e-4 and 1e-5)."""
+    from openusct_gb300 import problems
+    p = problems.gn3d(seed=0)
+    sl = [int(np.random.default_rng(2240).integers(p.n_shots))]
+    args = (p.geom, p.wavelet, p.dt, p.h, p.nt, p.v)
+    ref, born64 = oracle.gn_hessian_vector(p.m0, *args, src_list=sl, k=64, return_born=True)
+    hv, born = gb.gn_hessian_vector(p.m0, *args, src_list=sl, return_born=True)
+    assert rel_l2(born, born64) < 1e-5
+    assert rel_l2(hv, ref) < 1e-4
