@@ -371,16 +371,33 @@ def _setup(m, geom, h, dt, nt, src_list, footprints, mode, batch, ckpt_k, tile):
     return get_plan(shape, h, dt, nt, tx, rx, batch, ckpt_k or 0, *tile)
 
 
+def _drop_cached_workspaces():
+    """Let go of the workspaces plans keep between calls (a call in flight
+    holds its own references, so it is unaffected; later calls allocate
+    again)."""
+    with _LIVE_LOCK:
+        plans = list(_LIVE_PLANS)
+    for p in plans:
+        p._ws = {}
+
+
 def _alloc_bytes(nbytes, device):
     """A byte buffer on the device.  The interval a gradient sizes for itself
     counts the blocks torch has cached but not in use as available; one large
-    workspace cannot be carved from them, so on running out they are handed
-    back to the driver and the allocation is tried once more."""
+    workspace may not be carved from them, so on running out they are handed
+    back to the driver and the allocation is tried again, and then once more
+    after the workspaces other plans keep cached are let go as well."""
+    n = max(int(nbytes), 256)
     try:
-        return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+        return torch.empty(n, dtype=torch.uint8, device=device)
     except torch.cuda.OutOfMemoryError:
         torch.cuda.empty_cache()
-        return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+    try:
+        return torch.empty(n, dtype=torch.uint8, device=device)
+    except torch.cuda.OutOfMemoryError:
+        _drop_cached_workspaces()
+        torch.cuda.empty_cache()
+    return torch.empty(n, dtype=torch.uint8, device=device)
 
 
 def _workspace(nbytes, device):

@@ -410,3 +410,31 @@ def test_cpu_arm_memory_plan():
     bench.host_available_bytes = lambda: 197 << 30
     kg, _ = bench.cpu_shot_interval(prob, "gn")
     assert kg > 0
+
+
+def test_workspace_allocation_falls_back_to_releasing_caches(monkeypatch):
+    """A workspace that does not fit first releases torch's cached blocks, and
+    then the workspaces other plans keep between calls, before giving up."""
+    import torch
+    import openusct_gb300.backend as gb
+
+    class StandIn:
+        def __init__(self):
+            self._ws = {"grad": "held"}
+            gb._register_live(self)
+
+    other = StandIn()
+    calls = {"empty": 0, "cache": 0}
+
+    def fake_empty(n, dtype=None, device=None):
+        calls["empty"] += 1
+        if calls["empty"] < 3:
+            raise torch.cuda.OutOfMemoryError("out of memory")
+        return torch.zeros(n, dtype=dtype)
+
+    monkeypatch.setattr(gb.torch, "empty", fake_empty)
+    monkeypatch.setattr(gb.torch.cuda, "empty_cache",
+                        lambda: calls.__setitem__("cache", calls["cache"] + 1))
+    t = gb._alloc_bytes(1000, "cpu")
+    assert t.numel() == 1000 and calls == {"empty": 3, "cache": 2}
+    assert other._ws == {}
