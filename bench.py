@@ -379,19 +379,22 @@ def co_admission():
                             dt=base.dt, h=base.h, nt=base.nt, src_list=src))
     out = {}
     traces = {}
-    for name, merge in (("shared", True), ("separate", False)):
-        Engine(GpuExecutor(merge=merge), budget_bytes=150 << 30,
-               max_active=12).run_stream(reqs[:2], realtime=False)   # warm-up
-        eng = Engine(GpuExecutor(merge=merge), budget_bytes=150 << 30, max_active=12)
-        res = eng.run_stream(reqs, realtime=False)
-        st = summarize(res, eng)
-        out[name + "_shots_per_s"] = st.shots_per_s
-        out[name + "_groups"] = len({(r.t_admit, r.group) for r in res if r.ok})
-        traces[name] = [r.traces for r in res]
-    out["traces_equal"] = all(np.array_equal(a, b) for a, b in zip(traces["shared"],
-                                                                   traces["separate"]))
+    for slots in (12, 2):
+        for name, merge in (("shared", True), ("separate", False)):
+            Engine(GpuExecutor(merge=merge), budget_bytes=150 << 30,
+                   max_active=slots).run_stream(reqs[:2], realtime=False)   # warm-up
+            eng = Engine(GpuExecutor(merge=merge), budget_bytes=150 << 30, max_active=slots)
+            res = eng.run_stream(reqs, realtime=False)
+            st = summarize(res, eng)
+            key = f"{name}_{slots}_slots"
+            out[key + "_shots_per_s"] = st.shots_per_s
+            out[key + "_groups"] = len({(r.t_admit, r.group) for r in res if r.ok})
+            traces[key] = [r.traces for r in res]
+    ref = traces["separate_12_slots"]
+    out["traces_equal"] = all(all(np.array_equal(a, b) for a, b in zip(t, ref))
+                              for t in traces.values())
     out["stream"] = ("48 forward requests of 8 shots, 2D 256^2 ring (64 elements), nt=1500, each "
-                     "on its own perturbed model, arriving together; 12 slots")
+                     "on its own perturbed model, arriving together; 12 and 2 slots")
     return out
 
 
