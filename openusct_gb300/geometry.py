@@ -72,21 +72,33 @@ def element_csr(geom, shape, src_list=None, footprints=None):
     """
     idx = list(geom.idx) if hasattr(geom, "idx") else list(geom)
     n_el = len(idx)
-    if footprints is None:
-        groups = [([t], [1.0]) for t in idx]
-    else:
-        if len(footprints) != n_el:
-            raise ValueError("one footprint per element is required")
-        groups = [(list(c), list(w)) for c, w in footprints]
+    if footprints is not None and len(footprints) != n_el:
+        raise ValueError("one footprint per element is required")
     if src_list is None:
         src_list = list(range(n_el))
-    src_list = [int(s) for s in src_list]
-    for s in src_list:
+    src = np.asarray([int(s) for s in src_list], np.int64)
+    for s in src:
         if not 0 <= s < n_el:
             raise ValueError(f"src_list entry {s} outside 0..{n_el - 1}")
-    rx = _groups_csr(groups, shape)
-    tx = _groups_csr([groups[s] for s in src_list], shape)
-    return tx, rx
+    if n_el == 0:
+        rx = _groups_csr([], shape)
+    elif footprints is None:        # one cell of weight 1 per element
+        rx = CSR(np.arange(n_el + 1, dtype=np.int32), linear_indices(idx, shape),
+                 np.ones(n_el, np.float64))
+    else:
+        rx = _groups_csr([(list(c), list(w)) for c, w in footprints], shape)
+    return _select_rows(rx, src), rx
+
+
+def _select_rows(c: CSR, rows) -> CSR:
+    """The listed rows of ``c``, in the listed order (rows may repeat)."""
+    rows = np.asarray(rows, np.int64)
+    lens = (c.ptr[1:] - c.ptr[:-1])[rows].astype(np.int64)
+    ptr = np.zeros(len(rows) + 1, np.int64)
+    np.cumsum(lens, out=ptr[1:])
+    at = np.arange(int(ptr[-1]), dtype=np.int64) - np.repeat(ptr[:-1], lens) \
+        + np.repeat(c.ptr[:-1][rows].astype(np.int64), lens)
+    return CSR(ptr.astype(np.int32), c.cell[at].astype(np.int64), c.w[at].astype(np.float64))
 
 
 # ---------------------------------------------------------------------------

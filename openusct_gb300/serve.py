@@ -18,9 +18,9 @@ model, the observed data and every wavefield stay on the device across its
 iterations, and only scalars (misfits, CG dot products) reach the host until
 the final model.
 
-With ``GpuExecutor(merge=True)``, forward requests that share grid, spacing,
-time axis and wavelet (and have no sponge or footprints) are put in shared
-launches when more of them wait than there are free slots: when one is
+Forward requests that share grid, spacing, time axis and wavelet (and have
+no sponge or footprints) are put in shared launches when more of them wait
+than there are free slots (``GpuExecutor(merge=False)`` turns this off): when one is
 admitted, compatible requests already waiting join it (up to a batch of
 shots), and the group runs on one plan whose shot channels each carry their
 own model (``usct_plan_set_channel_models``).  Every request of a group gets
@@ -210,16 +210,41 @@ def _concat_csr(parts):
                np.concatenate([c.w for c in parts]))
 
 
+def _union_rows(parts):
+    """One CSR holding each distinct row of several element CSR lists once (a
+    row is its cells and weights), and per list the union row of each of its
+    rows: requests on the same elements share their receivers' traces."""
+    from .geometry import CSR
+    where, ptr, cells, ws, idx = {}, [0], [], [], []
+    for c in parts:
+        rows = []
+        for j in range(c.rows):
+            a, b = int(c.ptr[j]), int(c.ptr[j + 1])
+            cj, wj = np.asarray(c.cell[a:b]), np.asarray(c.w[a:b])
+            key = (cj.tobytes(), wj.tobytes())
+            if key not in where:
+                where[key] = len(ptr) - 1
+                ptr.append(ptr[-1] + (b - a))
+                cells.append(cj)
+                ws.append(wj)
+            rows.append(where[key])
+        idx.append(np.asarray(rows, np.int64))
+    cell = np.concatenate(cells) if cells else np.zeros(0, parts[0].cell.dtype)
+    w = np.concatenate(ws) if ws else np.zeros(0, parts[0].w.dtype)
+    return CSR(np.asarray(ptr, np.int32), cell, w), idx
+
+
 class GpuExecutor:
     """Runs one request on the GB300 engine on its own stream."""
 
     merge_width = 32   # shots of one launch group (a batch)
 
-    def __init__(self, device=None, graphs=False, workspace_bytes=None, merge=False):
+    def __init__(self, device=None, graphs=False, workspace_bytes=None, merge=True):
         import torch
         self.torch = torch
-        # compatible forward requests may share launches (measured slower than
-        # separate plans on concurrent streams on 2D streams, so off by default)
+        # compatible forward requests may share launches when they outnumber
+        # the free slots (one launch stream instead of several, each launch
+        # over up to a batch of shots)
         self.merge = merge
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.graphs = graphs
@@ -335,13 +360,14 @@ class GpuExecutor:
 
     def plan_for_group(self, reqs):
         """One plan for the transmits of all ``reqs`` (in order) and the union of
-        their receivers; transmit t uses the model of the request it came from."""
+        their receivers (each distinct receiver once); transmit t uses the model
+        of the request it came from."""
         from .backend import Plan
         from .geometry import element_csr
         shape = tuple(np.shape(reqs[0].m))
         parts = [element_csr(q.geom, shape, q.src_list, None) for q in reqs]
         tx = _concat_csr([t for t, _ in parts])
-        rx = _concat_csr([r for _, r in parts])
+        rx, rx_of = _union_rows([r for _, r in parts])
         C = self.merge_width
         q0 = reqs[0]
         plan = Plan(shape, q0.h, q0.dt, q0.nt, tx, rx, batch=C)
@@ -350,7 +376,7 @@ class GpuExecutor:
             plan.handle, len(reqs), owner.ctypes.data_as(_lib._ip)))
         if not self.graphs:
             plan.set("graphs", 0)
-        plan.group_parts = [(t.rows, r.rows) for t, r in parts]
+        plan.group_parts = [(t.rows, ix) for (t, _), ix in zip(parts, rx_of)]
         return plan
 
     def footprint_group(self, reqs, plan):
@@ -384,11 +410,10 @@ class GpuExecutor:
                                                   _lib.MODE_FORWARD, _ptr(data), s))
             plan.check(st)
             host = data.cpu().numpy()
-        out, t0, r0 = [], 0, 0
-        for nt_i, nr_i in plan.group_parts:
-            out.append({"traces": np.ascontiguousarray(host[t0:t0 + nt_i, :, r0:r0 + nr_i])})
+        out, t0 = [], 0
+        for nt_i, ix in plan.group_parts:
+            out.append({"traces": np.ascontiguousarray(host[t0:t0 + nt_i][:, :, ix])})
             t0 += nt_i
-            r0 += nr_i
         return out
 
     def _gauss_newton(self, req, plan, m, w, sp, mws, st):
@@ -491,20 +516,28 @@ class Engine:
     def _group_for(self, head, others, results):
         """Waiting requests that share ``head``'s launches, as (index, request)
         pairs starting with head; None for none.  Separate plans on their own
-        streams already overlap on the device, and a shared launch reads the
-        model once per shot, so requests are grouped only when more compatible
-        ones wait than there are free slots: ceil(waiting / free) requests per
-        group, in arrival order, their shots up to one batch."""
+        streams overlap on the device while slots are free, and a shared
+        launch reads the model once per shot, so requests are grouped only
+        when more compatible ones wait than there are free slots:
+        ceil(waiting / free) requests per group, in arrival order, their shots
+        up to one batch."""
         key_of = getattr(self.ex, "merge_key", None)
         if key_of is None:
             return None
+        keys = self._merge_keys          # each request's key, computed once
+
+        def key_for(j, q):
+            if j not in keys:
+                keys[j] = key_of(q)
+            return keys[j]
+
         i, rq = head
         width = getattr(self.ex, "merge_width", 32)
-        key = key_of(rq)
+        key = key_for(i, rq)
         if key is None or rq.n_shots >= width:
             return None
         cands = [it for it in sorted(others, key=lambda it: (it[0], it[1]))
-                 if not it[2].cancelled.is_set() and key_of(it[2]) == key]
+                 if not it[2].cancelled.is_set() and key_for(it[1], it[2]) == key]
         free = max(1, self.max_active - self.active)
         size = -(-(len(cands) + 1) // free)
         if size < 2:
@@ -526,6 +559,7 @@ class Engine:
         request order.  With ``realtime`` the arrival times are honoured."""
         reqs = sorted(enumerate(requests), key=lambda kv: kv[1].arrival)
         results = [None] * len(requests)
+        self._merge_keys = {}
         pending = []          # (arrival, order, req, plan, fp)
         threads = []
         t0 = time.perf_counter()
@@ -569,6 +603,7 @@ class Engine:
                 nxt += 1
             # admissions: first come first served, later ones may pass a head that
             # does not fit yet
+            drop = []            # plans to free once the lock is released
             with self.lock:
                 keep = []
                 while pending:
@@ -578,7 +613,7 @@ class Engine:
                         res = results[i]
                         res.error = "Cancelled: withdrawn before admission"
                         res.t_done = res.t_admit = time.perf_counter() - t0
-                        self.ex.release(plan)
+                        drop.append(plan)
                         done_count[0] += 1
                         continue
                     group = None
@@ -591,14 +626,14 @@ class Engine:
                             gfp = int(self.ex.footprint_group([q for _, q in group], gplan))
                         except Exception:
                             if gplan is not None:
-                                self.ex.release(gplan)
+                                drop.append(gplan)
                             gplan = None
                         if gplan is not None and self.reserved + gfp <= self.budget:
                             taken = {j for j, _ in group}
                             for it in pending + keep:
                                 if it[1] in taken:
-                                    self.ex.release(it[3])
-                            self.ex.release(plan)
+                                    drop.append(it[3])
+                            drop.append(plan)
                             pending[:] = [it for it in pending if it[1] not in taken]
                             heapq.heapify(pending)
                             keep = [it for it in keep if it[1] not in taken]
@@ -618,7 +653,7 @@ class Engine:
                             th.start()
                             continue
                         if gplan is not None:
-                            self.ex.release(gplan)
+                            drop.append(gplan)
                     if self.active < self.max_active and self.reserved + fp <= self.budget:
                         self.reserved += fp
                         self.active += 1
@@ -636,12 +671,18 @@ class Engine:
                         keep.append(item)
                 for item in keep:
                     heapq.heappush(pending, item)
-                if done_count[0] == len(reqs):
-                    break
-                wait = None
-                if nxt < len(reqs) and realtime:
-                    wait = max(0.0, reqs[nxt][1].arrival - (time.perf_counter() - t0))
-                self.lock.wait(timeout=wait if wait is not None else 0.05)
+                finished = done_count[0] == len(reqs)
+                if not finished and not drop:
+                    wait = None
+                    if nxt < len(reqs) and realtime:
+                        wait = max(0.0, reqs[nxt][1].arrival - (time.perf_counter() - t0))
+                    self.lock.wait(timeout=wait if wait is not None else 0.05)
+            # freeing device memory waits for the device: never under the lock,
+            # so admission does not stall behind running sweeps
+            for pl in drop:
+                self.ex.release(pl)
+            if finished:
+                break
         for th in threads:
             th.join()
         return results

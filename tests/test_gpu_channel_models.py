@@ -33,11 +33,11 @@ def _group_traces(eng, models, geoms, src_lists, c, C):
     """Traces of several requests through one plan with per-channel models."""
     _lib, gb = eng
     from openusct_gb300.geometry import element_csr
-    from openusct_gb300.serve import _concat_csr
+    from openusct_gb300.serve import _concat_csr, _union_rows
     shape = models[0].shape
     parts = [element_csr(g, shape, sl, None) for g, sl in zip(geoms, src_lists)]
     tx = _concat_csr([t for t, _ in parts])
-    rx = _concat_csr([r for _, r in parts])
+    rx, rx_of = _union_rows([r for _, r in parts])
     plan = gb.Plan(shape, c.h, c.dt, c.nt, tx, rx, batch=C)
     owner = np.concatenate([np.full(t.rows, i, np.int32) for i, (t, _) in enumerate(parts)])
     lib = _lib.load()
@@ -57,11 +57,10 @@ def _group_traces(eng, models, geoms, src_lists, c, C):
                                           s))
     plan.check()
     host = d.cpu().numpy()
-    out, t0, r0 = [], 0, 0
-    for t, r in parts:
-        out.append(host[t0:t0 + t.rows, :, r0:r0 + r.rows])
+    out, t0 = [], 0
+    for (t, _), ix in zip(parts, rx_of):
+        out.append(host[t0:t0 + t.rows][:, :, ix])
         t0 += t.rows
-        r0 += r.rows
     plan.close()
     return out
 
@@ -123,11 +122,11 @@ def test_served_forward_requests_share_launches_and_match_alone(eng):
         c[(yy - cy) ** 2 + (xx - cx) ** 2 <= 64] = 1580.0
         reqs.append(Request(kind="forward", m=1.0 / c ** 2, geom=ring, wavelet=wav, dt=dt, h=h,
                             nt=nt, src_list=list(range(k, k + 5)), arrival=0.001 * k))
-    ex = GpuExecutor(merge=True)
+    ex = GpuExecutor()                 # shared launches are the default
     mixed = Engine(ex, budget_bytes=20 << 30, max_active=1).run_stream(reqs, realtime=False)
     assert all(r.ok for r in mixed), [r.error for r in mixed]
     assert max(r.group for r in mixed) > 1
-    alone = [Engine(GpuExecutor(), budget_bytes=20 << 30, max_active=1).run_stream(
+    alone = [Engine(GpuExecutor(merge=False), budget_bytes=20 << 30, max_active=1).run_stream(
         [Request(kind="forward", m=q.m, geom=q.geom, wavelet=q.wavelet, dt=q.dt, h=q.h, nt=q.nt,
                  src_list=q.src_list)], realtime=False)[0] for q in reqs]
     for a, b in zip(mixed, alone):

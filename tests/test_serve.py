@@ -250,6 +250,23 @@ def test_concatenated_element_lists():
     assert list(rx.ptr) == [0, 1, 2, 3, 4, 5] and rx.rows == 5 and len(rx.w) == 5
 
 
+def test_receiver_union_keeps_each_distinct_row_once():
+    from openusct_gb300.geometry import element_csr
+    from openusct_gb300.serve import _union_rows
+    g1 = [(1, 2), (3, 4), (5, 6)]
+    g2 = [(5, 6), (7, 7)]
+    r1 = element_csr(g1, (8, 8), [0])[1]
+    r2 = element_csr(g1, (8, 8), [2])[1]      # the same elements: the same receivers
+    r3 = element_csr(g2, (8, 8), [0])[1]      # shares one element with g1
+    u, idx = _union_rows([r1, r2, r3])
+    assert u.rows == 4
+    assert [list(i) for i in idx] == [[0, 1, 2], [0, 1, 2], [2, 3]]
+    for r, ix in zip((r1, r2, r3), idx):
+        for j, k in enumerate(ix):
+            assert list(u.cell[u.ptr[k]:u.ptr[k + 1]]) == list(r.cell[r.ptr[j]:r.ptr[j + 1]])
+            assert list(u.w[u.ptr[k]:u.ptr[k + 1]]) == list(r.w[r.ptr[j]:r.ptr[j + 1]])
+
+
 def test_requests_are_grouped_only_when_they_outnumber_the_free_slots():
     ex = MergingExecutor()
     eng = Engine(ex, budget_bytes=10 ** 6, max_active=4)
