@@ -18,8 +18,9 @@ sampled during the timed region and the number of kernels launched.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Other workloads (not the default line): --workload ring2d (the 2D 256^2 ring,
-all 64 shots per launch), gn3d (the 224^3 Gauss-Newton Hessian-vector product),
+Other workloads (not the default line): --workload fmc3d (the forward FMC of
+the 192^3 cylinder acquisition: all 256 shots, nt=2000), ring2d (the 2D 256^2
+ring, all 64 shots per launch), gn3d (the 224^3 Gauss-Newton Hessian-vector product),
 grad3d_large (320^3, 512 shots, 8 per launch), tfm2d (the TFM image of a
 64 x 1500 x 64 FMC), invert2d (iterations of the device-resident inversion
 loop on the 2D ring).  --misfit gcn and --windows run the gradient workloads
@@ -160,6 +161,8 @@ def cpu_shot_interval(prob, mode, frac=0.65):
     import numpy as np
     N = int(np.prod(prob.shape))
     nt = prob.nt
+    if mode == "fwd":   # three levels in flight, no history
+        return 0, 3 * N * 8
     avail = host_available_bytes() or (64 << 30)
     budget = frac * avail
     hist = nt * N * 8
@@ -179,6 +182,13 @@ def cpu_whole_shot(prob, shot, k, dobs1=None, mode="grad", misfit="l2"):
     import numpy as np
     import oracle
     geom = prob.geom
+    grid = "x".join(str(v) for v in prob.shape)
+    if mode == "fwd":
+        t0 = time.perf_counter()
+        oracle.forward_fmc(prob.m_true, geom, prob.wavelet, prob.dt, prob.h, prob.nt, None,
+                           [shot])
+        return time.perf_counter() - t0, (f"1 whole shot ({prob.nt} levels) of the {grid} "
+                                          "forward FMC, every receiver recorded")
     if mode == "gn":
         t0 = time.perf_counter()
         oracle.gn_hessian_vector(prob.m0, geom, prob.wavelet, prob.dt, prob.h, prob.nt, prob.v,
@@ -189,7 +199,6 @@ def cpu_whole_shot(prob, shot, k, dobs1=None, mode="grad", misfit="l2"):
     oracle.misfit_and_gradient(prob.m0, geom, prob.wavelet, prob.dt, prob.h, prob.nt,
                                np.asarray(dobs1, np.float64), None, [shot], k=k,
                                misfit_type=misfit)
-    grid = "x".join(str(v) for v in prob.shape)
     plan = ("full history, no recompute (the reference core's memory plan)" if k == 0 else
             f"checkpoints every {k} steps (the full history does not fit this host)")
     return time.perf_counter() - t0, f"1 whole shot ({prob.nt} levels) of the {grid} gradient, {plan}"
@@ -412,7 +421,7 @@ def run_reference(args, prob, desc_w, mode):
     k, mem = cpu_shot_interval(prob, mode)
     shot = 0
     dobs1 = None
-    if mode != "gn":
+    if mode == "grad":
         dobs1 = oracle.forward_fmc(prob.m_true, prob.geom, prob.wavelet, prob.dt, prob.h,
                                    prob.nt, None, [shot])
     secs = []
@@ -423,7 +432,8 @@ def run_reference(args, prob, desc_w, mode):
             secs.append(s_i)
     ms = 1000.0 * sum(secs) / len(secs)
     value = 1000.0 / ms
-    line = {"metric": METRIC, "value": value, "unit": "shots/s", "n_gpus": args.gpus,
+    line = {"metric": FMC_METRIC if mode == "fwd" else METRIC, "value": value,
+            "unit": "shots/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
@@ -433,6 +443,162 @@ def run_reference(args, prob, desc_w, mode):
                              "seconds_per_step": [round(v, 3) for v in secs]},
             "e2e": {"value": value, "unit": "shots/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+FMC_METRIC = "Forward FMC shots/s (all transmits x all receivers x nt), same GB300, relerr<=1e-5"
+FMC_WORKLOAD = ("3D acoustic cylinder forward FMC, 192^3, dx=0.2mm, 8x32 elements (all 256 "
+                "shots), nt=2000, FP32 (the seeded random-field model); one step = the whole "
+                "acquisition, 256 x 2000 x 256 traces")
+
+
+def bench_fmc(args, prob):
+    """--workload fmc3d: the forward FMC of a whole acquisition (fwi.forward_fmc,
+    fwi.py:109-118) -- every transmit's forward sweep with every receiver
+    recorded, C shots per launch.  One step = all transmits."""
+    import ctypes
+    import numpy as np
+    import torch
+    from openusct_gb300 import _lib, backend
+    from openusct_gb300.geometry import element_csr
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_stream(torch.cuda.Stream(device=dev))
+    C = args.batch or 32
+    tx, rx = element_csr(prob.geom, prob.shape, None, None)
+    plan = backend.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx, rx, batch=C)
+    lib = _lib.load()
+    s = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    m = torch.from_numpy(prob.m_true).to(dev)
+    wav = torch.from_numpy(prob.wavelet).to(dev)
+    mws = torch.empty(plan.model_bytes(), dtype=torch.uint8, device=dev)
+    bws = torch.empty(plan.batch_bytes(_lib.MODE_FORWARD), dtype=torch.uint8, device=dev)
+    data = torch.empty((plan.n_tx, prob.nt, plan.n_rx), dtype=torch.float32, device=dev)
+
+    def step():
+        _lib.check(lib.usct_forward_fmc_dev(plan.handle, P(m), None, P(wav), P(data), P(mws),
+                                            P(bws), sp))
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    launches0 = plan.info("launches")
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        torch.cuda.synchronize()
+        ev0.record(s)
+        for _ in range(args.steps):
+            step()
+        ev1.record(s)
+        torch.cuda.synchronize()
+    launches = plan.info("launches") - launches0
+    t_ms = ev0.elapsed_time(ev1) / args.steps
+    value = plan.n_tx / (t_ms / 1000.0)
+    cells = int(np.prod(prob.shape))
+    hbm, peak_kind = _peaks()
+    # the forward stencil launch alone: two sweeps of one batch, traces not kept
+    nrep = 2
+    ev0.record(s)
+    for _ in range(nrep):
+        _lib.check(lib.usct_batch_forward(plan.handle, P(mws), P(bws), 0, _lib.MODE_FORWARD,
+                                          None, sp))
+    ev1.record(s)
+    torch.cuda.synchronize()
+    t_launch = ev0.elapsed_time(ev1) / 1000.0 / (nrep * (prob.nt - 1))
+    fwd_bytes = (12 * C + 4) * cells
+    achieved = fwd_bytes / t_launch / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "k_forward_tma_128cube_C32.md")
+    if C == 32 and os.path.exists(prof):
+        kv = {}
+        for line in open(prof):
+            if ":" in line and line.split(":")[0] in ("dram_bytes_per_launch", "cell_channels"):
+                kv[line.split(":")[0]] = float(line.split(":")[1])
+        if len(kv) == 2:
+            traffic = kv["dram_bytes_per_launch"] * (cells * C) / kv["cell_channels"]
+    nbatch = plan.nbatch
+    step_bytes = nbatch * (prob.nt - 1) * fwd_bytes + data.numel() * 4
+
+    # end to end through the public API: FP64 model and wavelet up, the FP64
+    # traces back to the host (the call's own return type)
+    del bws, data
+    torch.cuda.empty_cache()
+    call = lambda: backend.forward_fmc(prob.m_true, prob.geom, prob.wavelet, prob.dt,  # noqa
+                                       prob.h, prob.nt, batch=C)
+    out = call()
+    t0 = time.perf_counter()
+    ne = 2
+    for _ in range(ne):
+        out = call()
+    te = (time.perf_counter() - t0) / ne
+    e2e = {"value": plan.n_tx / te, "unit": "shots/s",
+           "h2d_bytes_per_step": int(prob.m_true.nbytes + prob.wavelet.nbytes),
+           "d2h_bytes_per_step": int(out.nbytes), "api": "openusct_gb300.backend.forward_fmc"}
+    del out
+    backend.release()
+
+    plain = None
+    if not args.no_plain:
+        torch.cuda.empty_cache()
+        tx1, rx1 = element_csr(prob.geom, prob.shape, [0], None)
+        pplan = backend.Plan(prob.shape, prob.h, prob.dt, prob.nt, tx1, rx1, batch=1)
+        pws = torch.empty(pplan.plain_bytes(False), dtype=torch.uint8, device=dev)
+        d1 = torch.empty((1, prob.nt, pplan.n_rx), dtype=torch.float32, device=dev)
+        args_p = (pplan.handle, P(m), P(wav), P(d1), P(pws), sp)
+        _lib.check(lib.usct_plain_forward_fmc_dev(*args_p))
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(3):   # the median of three timed calls
+            ev0.record(s)
+            _lib.check(lib.usct_plain_forward_fmc_dev(*args_p))
+            ev1.record(s)
+            torch.cuda.synchronize()
+            times.append(ev0.elapsed_time(ev1) / 1000.0)
+        tp = statistics.median(times)
+        plain = {"value": 1.0 / tp, "unit": "shots/s", "ms_per_shot": tp * 1000.0,
+                 "ms_per_shot_runs": [t * 1000.0 for t in times],
+                 "speedup_batched_vs_plain": value * tp}
+        del pws, d1
+        pplan.close()
+
+    cpu = None
+    if not args.no_cpu:
+        try:
+            import oracle
+            oracle.build()
+            secs, desc = cpu_whole_shot(prob, 0, 0, None, "fwd")
+            cpu = {"value": 1.0 / secs, "unit": "shots/s",
+                   "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+                   "kind": "port", "sample": desc, "seconds": secs}
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "error": str(exc)[:200]}
+
+    line = {"metric": FMC_METRIC, "value": value, "unit": "shots/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": t_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Gaussian random-field model)",
+            "config": {"workload": FMC_WORKLOAD, "grid": list(prob.shape), "nt": prob.nt,
+                       "shots": plan.n_tx, "receivers": plan.n_rx, "batch_shots": C,
+                       "tile": [plan.info("tile_x"), plan.info("tile_y"), plan.info("zchunk")],
+                       "parallelism": "single", "l2": "inputs larger than L2 (no flush needed)"},
+            "grid_updates_per_s": value * cells * (prob.nt - 1),
+            "roofline": {"bound": "hbm",
+                         "kernel": f"k_forward_tma (3D, {C} shots per launch)",
+                         "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
+                         "traffic_source": ("profiles/k_forward_tma_128cube_C32.md, scaled by "
+                                            "cell-channels" if traffic is not None else None),
+                         "algorithmic_bytes_per_launch": fwd_bytes,
+                         "launch_ms": t_launch * 1000.0},
+            "pipeline_roofline": {"bytes_per_step": step_bytes,
+                                  "achieved": step_bytes / (t_ms / 1000.0) / 1e9,
+                                  "frac": step_bytes / (t_ms / 1000.0) / 1e9 / hbm,
+                                  "model": f"12C+4 B per cell on {prob.nt - 1} levels of each of "
+                                           f"{nbatch} batches, plus the FP32 traces written"},
+            "e2e": e2e, "plain": plain, "cpu_baseline": cpu, "gpu_launches": launches,
+            "clocks": clk.summary()}
     print(json.dumps(line))
 
 
@@ -634,7 +800,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="grad3d",
-                    choices=sorted(WORKLOADS) + ["tfm2d", "invert2d"])
+                    choices=sorted(WORKLOADS) + ["fmc3d", "tfm2d", "invert2d"])
     ap.add_argument("--n", type=int, default=0, help="override the grid size (smaller variants)")
     ap.add_argument("--nt", type=int, default=0, help="override the time levels")
     ap.add_argument("--batch", type=int, default=0)
@@ -660,6 +826,19 @@ def main():
         import torch
         torch.cuda.set_device(0)
         (bench_tfm if args.workload == "tfm2d" else bench_invert)(args)
+        return
+
+    if args.workload == "fmc3d":
+        if rank != 0:
+            return
+        prob = problems.cylinder3d(seed=0, nt=args.nt or 2000)
+        desc = FMC_WORKLOAD if not args.nt else f"nt={prob.nt} variant of: " + FMC_WORKLOAD
+        if args.impl == "reference":
+            run_reference(args, prob, desc, "fwd")
+            return
+        import torch
+        torch.cuda.set_device(0)
+        bench_fmc(args, prob)
         return
 
     desc_w, build_prob, C0, k0, mode = WORKLOADS[args.workload]
