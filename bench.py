@@ -891,8 +891,14 @@ def main():
     m_true = torch.from_numpy(prob.m_true).to(dev)
     m0 = torch.from_numpy(prob.m0).to(dev)
     wav = torch.from_numpy(prob.wavelet).to(dev)
+    need = plan.batch_bytes(bmode)
+    free = torch.cuda.mem_get_info(dev)[0]
+    if need > 0.95 * free:
+        raise SystemExit(f"the {C}-shot batch workspace needs {need / 2**30:.0f} GiB even with the "
+                         f"smallest checkpoint plan (k = {plan.info('ckpt_k')}); "
+                         f"{free / 2**30:.0f} GiB are free: use a smaller --batch")
     mws = torch.empty(plan.model_bytes(), dtype=torch.uint8, device=dev)
-    bws = torch.empty(plan.batch_bytes(bmode), dtype=torch.uint8, device=dev)
+    bws = torch.empty(need, dtype=torch.uint8, device=dev)
     dobs = torch.empty((C, prob.nt, plan.n_rx), dtype=torch.float32, device=dev)
     # observed data from the true model (same engine, forward only)
     _lib.check(lib.usct_forward_fmc_dev(plan.handle, P(m_true), None, P(wav), P(dobs), P(mws),
