@@ -634,9 +634,25 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
     ok = wait_bar(bars + 1, 0u) && ok;
     float* lk_ptr = a.lk + (long long)z0 * g.PP + ro;
     double* g_row = has_g ? a.gacc + (long long)z0 * g.CPP + (long long)y * g.nxs + x0c : nullptr;
+    // C >= 4: a plane's per-lane shot sum is reduced across the cell's lanes
+    // and added to the gradient one iteration later, while that plane's stage
+    // is still resident (it is refilled only after the next plane's barrier),
+    // so the shuffle chain and the FP64 update overlap the next plane's
+    // stencil instead of holding up this plane's barrier; same arithmetic.
+    float s_def = 0.f;
+    double* g_def = nullptr;
+    const double* gs_def = nullptr;
+    auto flush = [&]() {
+        float s = s_def;
+        constexpr int G = C >= 4 ? C >> 2 : 1;
+        for (int o = 1; o < G; o <<= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
+        const int c0 = (4 * tx) >> logC;
+        if (own && (tx & (G - 1)) == 0) g_def[c0] = gs_def[c0] + (double)s;
+    };
     for (int z = z0; z < z1; ++z) {
         const int im = z - z0;
         ok = wait_bar(bars + s_p, ph_p) && ok;
+        if (C >= 4 && has_g && im > 0) flush();
         const float* sm_m = smf + (size_t)s_m * L.floats;
         const float* sm_c = smf + (size_t)s_c * L.floats;
         const float* sm_p = smf + (size_t)s_p * L.floats;
@@ -703,11 +719,9 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
                         make_double2(gs[c0] + (double)(pr[0] + pr[1]), gs[c0 + 1] + (double)(pr[2] + pr[3]));
                 }
             } else {
-                float s = (pr[0] + pr[1]) + (pr[2] + pr[3]);
-                const int G = C >> 2;
-                for (int o = 1; o < G; o <<= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
-                const int c0 = lf >> logC;
-                if (own && (tx & (G - 1)) == 0) grow[c0] = gs[c0] + (double)s;
+                s_def = (pr[0] + pr[1]) + (pr[2] + pr[3]);
+                g_def = grow;
+                gs_def = gs;
             }
         }
 
@@ -722,6 +736,9 @@ __global__ void __launch_bounds__(TXV* TY, (TXV * TY >= 256) ? 3 : 4) k_adjoint_
         s_c = s_p;
         if (++s_p == R) { s_p = 0; ph_p ^= 1u; }
     }
+    // the last plane's update: its stage is never refilled (no plane is
+    // issued after the last one's barrier)
+    if (ok && C >= 4 && has_g && z1 > z0) flush();
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);
         for (int i = (issued > R ? issued - R : 0); i < issued; ++i) (void)wait_stage(bars, i, R);
