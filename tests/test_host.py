@@ -59,6 +59,27 @@ def test_element_csr_footprints():
         assert list(rx.cell[a:b]) == list(geometry.linear_indices(cells, c["m0"].shape))
 
 
+def test_element_csr_rows_are_the_elements_rows():
+    """Transmit row i is receiver row src_list[i] (cells, weights, dtypes), for
+    point elements and footprints, repeated and reordered transmits, 2D and 3D."""
+    c = load("ring2d_aperture")
+    g3 = geometry.IndexGeometry([(1, 2, 3), (4, 4, 4), (0, 5, 6)])
+    cases = [(c.geom, c["m0"].shape, [3, 1, 3, 0], None),
+             (c.geom, c["m0"].shape, c.src_list[::-1] + c.src_list[:2], c.footprints),
+             (c.geom, c["m0"].shape, [], c.footprints),
+             (g3, (5, 6, 7), None, None)]
+    for geom, shape, src, fp in cases:
+        tx, rx = geometry.element_csr(geom, shape, src, fp)
+        src = list(range(rx.rows)) if src is None else src
+        assert tx.ptr.dtype == np.int32 and tx.cell.dtype == np.int64 and tx.w.dtype == np.float64
+        assert tx.rows == len(src) and tx.ptr[0] == 0
+        for i, s in enumerate(src):
+            a, b = tx.ptr[i], tx.ptr[i + 1]
+            ra, rb = rx.ptr[s], rx.ptr[s + 1]
+            assert np.array_equal(tx.cell[a:b], rx.cell[ra:rb])
+            assert np.array_equal(tx.w[a:b], rx.w[ra:rb])
+
+
 def test_batch_choice_respects_budget():
     shape, nt = (192, 192, 192), 2000
     full = batch_bytes_estimate(shape, nt, 256, 256, 32, 64, 1)
