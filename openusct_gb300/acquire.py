@@ -71,6 +71,17 @@ class Dataset:
     def dt(self):
         return 1.0 / self.sample_rate_hz
 
+    def save(self, path):
+        """Write the platform's HDF5 Dataset file (dataset.py:112-140)."""
+        from .dataset_io import save
+        save(self, path)
+
+    @classmethod
+    def load(cls, path):
+        """Read a Dataset file (dataset.py:142-174)."""
+        from .dataset_io import load
+        return load(path)
+
 
 def _classes():
     try:

@@ -1,0 +1,261 @@
+"""Acquisition files without h5py: the Dataset layout and the UDSP v4.0 Set.
+
+The round trips restate the reference's own tests (simulation/tests/
+test_dataset.py: 2D and 3D, ground truth kept; simulation/tests/
+test_uarp_format.py: data, geometry, timing and transmit map kept, and the
+UDSP group layout present).  No HDF5 implementation exists here to check the
+files against, so the format tests pin the structures themselves: the
+superblock, variable-length strings in a global heap, B-trees of several
+levels (small node ranks) and sibling links, chunked gzip data with an edge
+chunk, and a user block before the superblock.
+"""
+
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from openusct_gb300 import dataset_io, hdf5
+from openusct_gb300.acquire import ArrayGeometry, Dataset
+
+
+def _ring_dataset(n_tx=3, nt=300, n_el=8, truth=True, seed=0):
+    rng = np.random.default_rng(seed)
+    ang = np.linspace(0, 2 * np.pi, n_el, endpoint=False)
+    pos = 0.024 * np.column_stack([np.cos(ang), np.sin(ang)])
+    c = 1480.0 + 20.0 * rng.standard_normal((61, 61))
+    return Dataset(geometry=ArrayGeometry(pos, 0.024, 0.4e6, "ring"),
+                   data=rng.standard_normal((n_tx, nt, n_el)) * 1e-3, sample_rate_hz=1 / 1.2e-7,
+                   tx_wavelet=rng.standard_normal(nt), tx_centre_freq_hz=0.41e6,
+                   nominal_speed_m_s=1480.0, tx_elements=[0, 2, 4][:n_tx],
+                   ground_truth={"c": c, "h_m": 1e-3} if truth else None,
+                   metadata={"description": "roundtrip test", "created_by": "tests"})
+
+
+def _cylinder_dataset(src=(0, 6), nt=120):
+    rng = np.random.default_rng(1)
+    zs = np.linspace(-0.005, 0.005, 2)
+    ang = np.linspace(0, 2 * np.pi, 6, endpoint=False)
+    pos = np.array([[0.012 * np.cos(a), 0.012 * np.sin(a), z] for z in zs for a in ang])
+    c = 1480.0 + rng.standard_normal((16, 16, 16))
+    return Dataset(geometry=ArrayGeometry(pos, 0.012, 0.3e6, "cylinder"),
+                   data=rng.standard_normal((len(src), nt, 12)), sample_rate_hz=5e6,
+                   tx_wavelet=rng.standard_normal(nt), tx_centre_freq_hz=0.3e6,
+                   nominal_speed_m_s=1480.0, tx_elements=list(src),
+                   ground_truth={"c": c, "h_m": 2e-3})
+
+
+def test_dataset_roundtrip_2d(tmp_path):
+    ds = _ring_dataset()
+    path = str(tmp_path / "ds.h5")
+    ds.save(path)
+    got = Dataset.load(path)
+    assert got.data.dtype == np.float32 and got.data.shape == (3, 300, 8)
+    assert np.array_equal(got.data, ds.data.astype(np.float32))
+    assert np.array_equal(got.geometry.element_pos, ds.geometry.element_pos)
+    assert got.geometry.dim == 2 and got.geometry.n_elements == 8
+    assert got.geometry.array_type == "ring" and got.geometry.radius_m == 0.024
+    assert got.geometry.centre_freq_hz == 0.4e6
+    assert got.sample_rate_hz == ds.sample_rate_hz and got.nominal_speed_m_s == 1480.0
+    assert got.tx_centre_freq_hz == 0.41e6
+    assert np.array_equal(got.tx_wavelet, ds.tx_wavelet)
+    assert list(got.tx_elements) == [0, 2, 4]
+    assert np.array_equal(got.ground_truth["c"], ds.ground_truth["c"])
+    assert got.ground_truth["h_m"] == 1e-3
+    assert got.metadata == {"description": "roundtrip test", "created_by": "tests",
+                            "format_version": "1.0"}
+
+
+def test_dataset_roundtrip_3d_and_without_truth(tmp_path):
+    ds = _cylinder_dataset()
+    path = str(tmp_path / "ds3d.h5")
+    dataset_io.save(ds, path)
+    got = dataset_io.load(path)
+    assert got.geometry.dim == 3 and got.geometry.element_pos.shape == (12, 3)
+    assert np.array_equal(got.data, ds.data.astype(np.float32))
+    assert got.ground_truth["c"].shape == (16, 16, 16)
+    assert np.array_equal(got.ground_truth["c"], ds.ground_truth["c"])
+    bare = _ring_dataset(truth=False)
+    dataset_io.save(bare, path, compression=None)
+    got = dataset_io.load(path)
+    assert got.ground_truth is None and np.array_equal(got.data, bare.data.astype(np.float32))
+    with hdf5.File(path, "r") as f:
+        assert "ground_truth" not in f and f["acquisition/data"].compression is None
+
+
+def test_dataset_layout_is_the_schema(tmp_path):
+    path = str(tmp_path / "ds.h5")
+    dataset_io.save(_ring_dataset(), path)
+    with hdf5.File(path, "r") as f:
+        assert sorted(f.keys()) == ["acquisition", "geometry", "ground_truth"]
+        assert f.attrs["format_version"] == "1.0" and isinstance(f.attrs["description"], str)
+        g = f["geometry"]
+        assert sorted(g.attrs.keys()) == ["array_type", "centre_freq_hz", "n_elements", "radius_m"]
+        assert g.attrs["n_elements"] == 8 and g.attrs["n_elements"].dtype == np.int64
+        assert g["element_pos"].dtype == np.float64 and g["element_pos"].shape == (8, 2)
+        a = f["acquisition"]
+        assert sorted(a.keys()) == ["data", "tx_elements", "tx_wavelet"]
+        assert a["data"].dtype == np.float32 and a["data"].compression == "gzip"
+        assert a["tx_elements"].dtype == np.int64
+        assert f["ground_truth"]["c"].compression == "gzip"
+
+
+def test_unknown_major_version_is_refused(tmp_path):
+    path = str(tmp_path / "v2.h5")
+    with hdf5.File(path, "w") as f:
+        f.attrs["format_version"] = "2.0"
+    with pytest.raises(ValueError, match="format_version"):
+        dataset_io.load(path)
+
+
+def test_uarp_roundtrip_and_layout(tmp_path):
+    ds = _cylinder_dataset(src=(0, 4, 8, 11), nt=120)
+    path = str(tmp_path / "acq_udsp.h5")
+    dataset_io.to_uarp_set(ds, path)
+    with hdf5.File(path, "r") as f:
+        assert f.attrs["Version"] == "4.0"
+        s0 = f["Series/Series000"]
+        assert "Dimensions/Value" in s0
+        assert float(s0["Dimensions/Dimension1"].attrs["Uniform.Stride"]) == 1 / 5e6
+        assert "Dimensions/Dimension2/Sparse.Points" in s0
+        assert int(s0["Frames"].attrs["Size"]) == 4
+        assert "Frames/Frame000000" in s0
+        assert s0["Frames/Frame000003"].attrs["Description"] == "tx_element=11"
+        assert s0.attrs["State"] == "Analytical"
+    got = dataset_io.from_uarp_set(path)
+    assert got.n_tx == 4 and got.n_samples == 120 and got.geometry.dim == 3
+    assert np.array_equal(got.data, ds.data.astype(np.float32))
+    assert np.array_equal(got.geometry.element_pos, ds.geometry.element_pos)
+    assert abs(got.dt - 1 / 5e6) < 1e-15
+    assert list(got.tx_elements) == [0, 4, 8, 11]
+    assert got.geometry.array_type == "cylinder"
+    assert np.isclose(got.geometry.radius_m, np.linalg.norm(ds.geometry.element_pos, axis=1).max())
+
+
+def test_superblock_and_strings_are_the_earliest_format(tmp_path):
+    path = str(tmp_path / "s.h5")
+    with hdf5.File(path, "w") as f:
+        f.attrs["text"] = "ring"
+        f.attrs["empty"] = ""
+        f.attrs["fixed"] = b"abc"
+        f.attrs["labels"] = np.array(["a", "bc"])
+        f.attrs["ints"] = np.arange(3, dtype=np.int32)
+        f.create_group("g")
+        f.create_dataset("scalar", data=np.float64(3.5))
+        f.create_dataset("empty", data=np.zeros((0, 3)))
+        f.create_dataset("strided", data=np.arange(12, dtype=np.int16).reshape(3, 4)[:, ::2])
+    raw = open(path, "rb").read()
+    assert raw[:8] == hdf5.SIGNATURE
+    assert raw[8:16] == bytes([0, 0, 0, 0, 0, 8, 8, 0])          # version 0, 8-byte offsets
+    leaf_k, internal_k = struct.unpack("<HH", raw[16:20])
+    assert leaf_k >= 4 and internal_k == 16
+    assert struct.unpack("<Q", raw[40:48])[0] == len(raw)        # end of file
+    assert b"GCOL" in raw and b"TREE" in raw and b"HEAP" in raw and b"SNOD" in raw
+    oh = struct.unpack("<Q", raw[64:72])[0]                       # the root entry's header
+    assert raw[oh] == 1                                           # version-1 object header
+    with hdf5.File(path, "r") as f:
+        assert f.attrs["text"] == "ring" and isinstance(f.attrs["text"], str)
+        assert f.attrs["empty"] == ""
+        assert f.attrs["fixed"] == b"abc" and isinstance(f.attrs["fixed"], np.bytes_)
+        assert list(f.attrs["labels"]) == ["a", "bc"]
+        assert f.attrs["ints"].dtype == np.int32 and list(f.attrs["ints"]) == [0, 1, 2]
+        assert f.keys() == ["empty", "g", "scalar", "strided"] and f["g"].keys() == []
+        assert f["scalar"].shape == () and f["scalar"][()] == 3.5
+        assert f["empty"][()].shape == (0, 3)
+        assert f["strided"][()].tolist() == [[0, 2], [4, 6], [8, 10]]
+
+
+def test_deep_btrees_and_edge_chunks(tmp_path, monkeypatch):
+    """Small node ranks force several symbol-table nodes and B-tree levels;
+    small chunks force a chunk B-tree of several levels and a partial last
+    chunk: everything reads back in order and unchanged."""
+    monkeypatch.setattr(hdf5, "_CHUNK_BYTES", 4 * 7 * 5)       # 5 rows of 7 FP32 per chunk
+    path = str(tmp_path / "deep.h5")
+    rng = np.random.default_rng(2)
+    big = rng.standard_normal((333, 7)).astype(np.float32)      # 67 chunks, the last partial
+    arrays = {f"Frame{i:06d}": rng.standard_normal((3, 2)) for i in range(41)}
+    with hdf5.File(path, "w", leaf_k=2, internal_k=2) as f:
+        fr = f.create_group("Frames")
+        for k, v in arrays.items():
+            fr.create_dataset(k, data=v)
+        f.create_dataset("big", data=big, compression="gzip")
+    with hdf5.File(path, "r") as f:
+        assert f["Frames"].keys() == sorted(arrays)
+        for k, v in arrays.items():
+            assert np.array_equal(f["Frames"][k][()], v)
+        assert f["big"].chunks == (5, 7)
+        assert np.array_equal(f["big"][()], big)
+
+
+def test_btree_leaves_are_linked_by_siblings(tmp_path):
+    """Readers that walk a B-tree's leaf level through right-sibling links
+    (instead of descending every child) find the same symbol-table nodes."""
+    path = str(tmp_path / "sib.h5")
+    with hdf5.File(path, "w", leaf_k=1, internal_k=2) as f:
+        for i in range(37):
+            f.create_group(f"g{i:03d}")
+    raw = open(path, "rb").read()
+    bt = struct.unpack("<Q", raw[80:88])[0]            # root entry scratch: B-tree
+    q = lambda a: struct.unpack("<Q", raw[a:a + 8])[0]  # noqa: E731
+
+    def node(a):
+        assert raw[a:a + 4] == b"TREE" and raw[a + 4] == 0
+        level, n = raw[a + 5], struct.unpack("<H", raw[a + 6:a + 8])[0]
+        left, right = q(a + 8), q(a + 16)
+        kids = [q(a + 24 + 8 + 16 * i) for i in range(n)]
+        return level, left, right, kids
+
+    def descend(a):
+        level, _, _, kids = node(a)
+        return [a] if level == 0 else [x for k in kids for x in descend(k)]
+
+    leaves = descend(bt)
+    assert len(leaves) > 2
+    level, left, right, _ = node(bt)
+    a = bt
+    while node(a)[0] > 0:
+        a = node(a)[3][0]
+    walked = []
+    while a != hdf5.UNDEF:
+        walked.append(a)
+        a = node(a)[2]
+    assert walked == leaves
+    assert node(leaves[0])[1] == hdf5.UNDEF
+    assert all(node(leaves[i])[1] == leaves[i - 1] for i in range(1, len(leaves)))
+    names = []
+    for leaf in leaves:
+        for snod in node(leaf)[3]:
+            assert raw[snod:snod + 4] == b"SNOD"
+            names.append(struct.unpack("<H", raw[snod + 6:snod + 8])[0])
+    assert sum(names) == 37
+    with hdf5.File(path, "r") as f:
+        assert f.keys() == [f"g{i:03d}" for i in range(37)]
+
+
+def test_user_block_before_the_superblock(tmp_path):
+    path = str(tmp_path / "plain.h5")
+    dataset_io.save(_ring_dataset(), path)
+    shifted = str(tmp_path / "shifted.h5")
+    with open(shifted, "wb") as out:
+        out.write(b"\0" * 512 + open(path, "rb").read())
+    got = dataset_io.load(shifted)
+    assert np.array_equal(got.data, _ring_dataset().data.astype(np.float32))
+
+
+def test_errors_are_reported(tmp_path):
+    with pytest.raises(ValueError, match="not an HDF5 file"):
+        p = tmp_path / "x.h5"
+        p.write_bytes(b"nope" * 100)
+        hdf5.File(str(p), "r")
+    with hdf5.File(str(tmp_path / "e.h5"), "w") as f:
+        with pytest.raises(NotImplementedError):
+            f.create_dataset("s", data=np.array(["a"]))
+        with pytest.raises(NotImplementedError):
+            f.create_dataset("z", data=np.zeros(3), compression="lzf")
+    # a failed write leaves no file behind
+    with pytest.raises(RuntimeError):
+        with hdf5.File(str(tmp_path / "never.h5"), "w") as f:
+            f.attrs["a"] = 1
+            raise RuntimeError("stop")
+    assert not os.path.exists(tmp_path / "never.h5")
