@@ -259,3 +259,39 @@ def test_errors_are_reported(tmp_path):
             f.attrs["a"] = 1
             raise RuntimeError("stop")
     assert not os.path.exists(tmp_path / "never.h5")
+
+
+REF = os.path.join(os.environ.get("USCT_REFERENCE", ""), "simulation") \
+    if os.environ.get("USCT_REFERENCE") else ""
+
+
+@pytest.mark.skipif(not REF or not os.path.isdir(REF),
+                    reason="USCT_REFERENCE does not name the reference checkout")
+def test_reference_dataset_objects_round_trip(tmp_path):
+    """The reference's own Dataset and ArrayGeometry (built by its
+    constructors) go through both file layouts, and the readers hand back the
+    reference's classes."""
+    import sys
+    sys.path.insert(0, REF)
+    from ringfwi.dataset import ArrayGeometry as RG, Dataset as RD
+    rng = np.random.default_rng(4)
+    geom = RG.cylinder(2, 6, 0.012, 0.010, 0.3e6)
+    ds = RD(geometry=geom, data=rng.standard_normal((4, 50, 12)), sample_rate_hz=5e6,
+            tx_wavelet=rng.standard_normal(50), tx_centre_freq_hz=0.3e6, nominal_speed_m_s=1480.0,
+            tx_elements=[0, 4, 8, 11], ground_truth={"c": rng.standard_normal((9, 9, 9)),
+                                                     "h_m": 2e-3},
+            metadata={"description": "ref objects"})
+    p = str(tmp_path / "ref.h5")
+    dataset_io.save(ds, p)
+    got = dataset_io.load(p)
+    assert type(got) is RD and type(got.geometry) is RG
+    assert np.array_equal(got.data, ds.data.astype(np.float32))
+    assert np.array_equal(got.geometry.element_pos, geom.element_pos)
+    assert got.geometry.array_type == "cylinder" and got.geometry.dim == 3
+    assert list(got.tx_elements) == [0, 4, 8, 11]
+    assert got.metadata["description"] == "ref objects" and got.metadata["created_by"] == "OpenUSCT"
+    q = str(tmp_path / "ref_udsp.h5")
+    dataset_io.to_uarp_set(ds, q)
+    back = dataset_io.from_uarp_set(q)
+    assert type(back) is RD and list(back.tx_elements) == [0, 4, 8, 11]
+    assert np.array_equal(back.data, ds.data.astype(np.float32))
