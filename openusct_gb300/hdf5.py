@@ -575,37 +575,28 @@ class _Reader:
             q += 1
         return bytes(b[p:q]).decode("utf-8")
 
-    def _btree_children(self, at, node_type):
-        """(left key offset, child address, level-0) leaves of a v1 B-tree, in order."""
+    def _btree_children(self, at, node_type, key_size):
+        """[(left key position, child address)] of the leaves of a version-1
+        B-tree, in key order (every child descended, so sibling links are not
+        needed)."""
         b = self.b
         if bytes(b[at:at + 4]) != b"TREE" or b[at + 4] != node_type:
             raise ValueError("bad B-tree node")
         level, n = b[at + 5], self.u(at + 6, 2)
-        ks = self.L if node_type == 0 else None
         p = at + 8 + 2 * self.O
         out = []
-        if node_type == 0:
-            for i in range(n):
-                child = self.addr(p + ks)
-                if level > 0:
-                    out.extend(self._btree_children(child, 0))
-                else:
-                    out.append((p, child))
-                p += ks + self.O
-        else:
-            ks = self._chunk_key_size
-            for i in range(n):
-                child = self.addr(p + ks)
-                if level > 0:
-                    out.extend(self._btree_children(child, 1))
-                else:
-                    out.append((p, child))
-                p += ks + self.O
+        for _ in range(n):
+            child = self.addr(p + key_size)
+            if level > 0:
+                out.extend(self._btree_children(child, node_type, key_size))
+            else:
+                out.append((p, child))
+            p += key_size + self.O
         return out
 
     def _stab(self, bt, heap, out):
         b = self.b
-        for _, snod in self._btree_children(bt, 0):
+        for _, snod in self._btree_children(bt, 0, self.L):
             if bytes(b[snod:snod + 4]) != b"SNOD":
                 raise ValueError("bad symbol table node")
             n = self.u(snod + 6, 2)
@@ -836,9 +827,8 @@ class _Reader:
         out = np.zeros(shape, dt.newbyteorder("="))
         if bt is None:
             return out
-        self._chunk_key_size = 8 + 8 * (rank + 1)
         filters = info["filters"]
-        leaves = self._btree_children(bt, 1)
+        leaves = self._btree_children(bt, 1, 8 + 8 * (rank + 1))
 
         def one(leaf):
             kp, child = leaf
