@@ -214,12 +214,13 @@ def test_time_weights_unit_window_is_identity_and_mute_reduces_misfit():
     assert rel_l2(g2, g0) > 1e-2     # (the gradient entries are far below allclose's atol)
 
 
-def test_pipeline_simulate_then_fwi_plugin():
-    """simulation/tests/test_pipeline.py:23-59 without the HDF5 round trip (no
-    h5py): simulate the acquisition with openusct_gb300.acquire, reconstruct it
-    through the "fwi" plugin entry (openusct_gb300.invert.fwi_from_dataset)
-    from the flaw-free background; the misfit halves and the flaw is recovered
-    slower than the background, as the reference's run does (pipeline2d)."""
+def test_pipeline_simulate_then_fwi_plugin(tmp_path):
+    """simulation/tests/test_pipeline.py:23-59: simulate the acquisition with
+    openusct_gb300.acquire, round-trip it through the portable HDF5 file
+    (openusct_gb300.dataset_io; FP32 traces on disk), reconstruct it through
+    the "fwi" plugin entry (openusct_gb300.invert.fwi_from_dataset) from the
+    flaw-free background; the misfit halves and the flaw is recovered slower
+    than the background, as the reference's run does (pipeline2d)."""
     from openusct_gb300.acquire import simulate_dataset
     from openusct_gb300.geometry import IndexGeometry
     from openusct_gb300.invert import fwi_from_dataset, register
@@ -235,7 +236,11 @@ def test_pipeline_simulate_then_fwi_plugin():
     ds = simulate_dataset(z["c_true"], ring, z["wavelet"], float(z["dt"]),
                           nominal_speed_m_s=3000.0)
     assert rel_l2(ds.data, z["data"]) < 1e-5
-    res = fwi_from_dataset(ds, start_c=z["c_bg"], m_bounds=(float(z["lo"]), float(z["hi"])),
+    path = str(tmp_path / "acq.h5")
+    ds.save(path)
+    loaded = type(ds).load(path)
+    assert np.array_equal(loaded.data, ds.data.astype(np.float32))
+    res = fwi_from_dataset(loaded, start_c=z["c_bg"], m_bounds=(float(z["lo"]), float(z["hi"])),
                            n_iter=6, step_frac=0.04)
     hist = res["history"]
     assert hist[-1] < 0.5 * hist[0]
