@@ -522,10 +522,11 @@ class _Reader:
                     mtype, size, mflags = self.u(p, 2), self.u(p + 2, 2), b[p + 4]
                     p += 8
                 else:
-                    if p + 4 > end - 4:                  # the chunk ends with a checksum
+                    hdr = 4 + (2 if oflags & 0x04 else 0)
+                    if p + hdr > end:                    # a gap shorter than a header
                         break
                     mtype, size, mflags = b[p], self.u(p + 1, 2), b[p + 3]
-                    p += 4 + (2 if oflags & 0x04 else 0)
+                    p += hdr
                 body = b[p:p + size]
                 p += size
                 if mflags & 0x02:
@@ -535,8 +536,8 @@ class _Reader:
                     cl = int.from_bytes(body[self.O:self.O + self.L], "little")
                     if ver == 1:
                         chunks.append((ca, ca + cl, 1, 0))
-                    else:
-                        chunks.append((ca + 4, ca + cl, 2, oflags))   # "OCHK" ... checksum
+                    else:                                # "OCHK", messages, checksum
+                        chunks.append((ca + 4, ca + cl - 4, 2, oflags))
                     continue
                 out.append((mtype, body, mflags))
         return out

@@ -295,3 +295,104 @@ def test_reference_dataset_objects_round_trip(tmp_path):
     back = dataset_io.from_uarp_set(q)
     assert type(back) is RD and list(back.tx_elements) == [0, 4, 8, 11]
     assert np.array_equal(back.data, ds.data.astype(np.float32))
+
+
+def test_reader_takes_structures_the_writer_does_not_emit(tmp_path):
+    """A file built byte by byte from the format's structures that newer
+    writers use: superblock version 2; version-2 object headers whose link
+    messages make a compact group; a compact layout; version-3 attribute and
+    version-2 dataspace messages; a version-1 header continued in a second
+    block; a chunked dataset through shuffle + deflate (version-2 filter
+    pipeline) with a partial last chunk."""
+    import zlib
+    buf = bytearray(48)
+
+    def put(data):
+        while len(buf) % 8:
+            buf.append(0)
+        a = len(buf)
+        buf.extend(data)
+        return a
+
+    class Sink:                  # hdf5._btree's allocator over this buffer
+        alloc = staticmethod(put)
+
+        @staticmethod
+        def patch(a, d):
+            buf[a:a + len(d)] = d
+
+    def ohdr2(msgs):
+        body = b"".join(struct.pack("<BHB", t, len(m), 0) + m for t, m in msgs)
+        return b"OHDR" + bytes([2, 0x02]) + struct.pack("<I", len(body)) + body + b"\0" * 4
+
+    def ohdr1(msgs, n_total):
+        body = b"".join(struct.pack("<HHB3x", t, len(hdf5._pad8(m)), 0) + hdf5._pad8(m)
+                        for t, m in msgs)
+        return struct.pack("<BBHII4x", 1, 0, n_total, 1, len(body)) + body, body
+
+    def space2(shape):
+        return struct.pack("<BBBB", 2, len(shape), 0, 1) + b"".join(struct.pack("<Q", s)
+                                                                      for s in shape)
+
+    def attr3(name, dt, sp, data):
+        nm = name.encode() + b"\0"
+        return struct.pack("<BBHHHB", 3, 0, len(nm), len(dt), len(sp), 0) + nm + dt + sp + data
+
+    f4, f8, i2, i8 = (hdf5._dtype_message(np.dtype(t)) for t in ("<f4", "<f8", "<i2", "<i8"))
+    a = np.arange(6, dtype=np.float32).reshape(2, 3) / 7
+    compact = put(ohdr2([
+        (0x01, space2(a.shape)), (0x03, f4),
+        (0x08, struct.pack("<BBH", 3, 0, a.nbytes) + a.tobytes()),
+        (0x0C, attr3("units", hdf5._dtype_message(np.dtype("S3")), space2(()), b"m/s")),
+        (0x0C, attr3("n", i8, space2(()), struct.pack("<q", 7)))]))
+    b = np.linspace(0, 1, 4)
+    data_b = put(b.tobytes())
+    cont_msgs = [(0x03, f8), (0x08, struct.pack("<BBQQ", 3, 1, data_b, b.nbytes)),
+                 (0x0C, hdf5._attr_message("scale", 2.5, None))]
+    _, cont_body = ohdr1(cont_msgs, 0)
+    cont = put(cont_body)
+    continued, _ = ohdr1([(0x01, hdf5._space_message(b.shape)),
+                          (0x10, struct.pack("<QQ", cont, len(cont_body)))], 5)
+    continued = put(continued)
+    c = (np.arange(10, dtype=np.int16) * 1000 - 4321)
+    children, keys = [], []
+    for i in range(3):
+        part = np.zeros(4, np.int16)
+        seg = c[4 * i:4 * i + 4]
+        part[:len(seg)] = seg
+        shuffled = np.frombuffer(part.tobytes(), np.uint8).reshape(-1, 2).T.tobytes()
+        blob = zlib.compress(shuffled, 6)
+        children.append(put(blob))
+        keys.append(struct.pack("<II", len(blob), 0) + struct.pack("<QQ", 4 * i, 0))
+    keys.append(struct.pack("<II", 0, 0) + struct.pack("<QQ", 12, 2))
+    bt = hdf5._btree(Sink, 1, children, keys, 24, 32)
+    pipeline = (struct.pack("<BB", 2, 2) + struct.pack("<HHH", 2, 0, 1) + struct.pack("<I", 2) +
+                struct.pack("<HHH", 1, 0, 1) + struct.pack("<I", 6))
+    chunked = put(ohdr2([(0x01, space2(c.shape)), (0x03, i2),
+                         (0x08, struct.pack("<BBBQ", 3, 2, 2, bt) + struct.pack("<2I", 4, 2)),
+                         (0x0B, pipeline)]))
+
+    def link(name, addr):
+        nm = name.encode()
+        return struct.pack("<BBB", 1, 0, len(nm)) + nm + struct.pack("<Q", addr)
+
+    root = put(ohdr2([(0x06, link("compact", compact)), (0x06, link("continued", continued)),
+                      (0x06, link("chunked", chunked)),
+                      (0x0C, attr3("title", hdf5._dtype_message(np.dtype("S4")), space2(()),
+                                   b"demo"))]))
+    while len(buf) % 8:
+        buf.append(0)
+    buf[:48] = (hdf5.SIGNATURE + struct.pack("<BBBB", 2, 8, 8, 0) +
+                struct.pack("<QQQQ", 0, hdf5.UNDEF, len(buf), root) + b"\0" * 4)
+    path = tmp_path / "newer.h5"
+    path.write_bytes(bytes(buf))
+    with hdf5.File(str(path), "r") as f:
+        assert f.keys() == ["chunked", "compact", "continued"]
+        assert f.attrs["title"] == b"demo"
+        assert np.array_equal(f["compact"][()], a)
+        assert f["compact"].attrs["units"] == b"m/s" and f["compact"].attrs["n"] == 7
+        assert np.array_equal(f["continued"][()], b)
+        assert f["continued"].attrs["scale"] == 2.5
+        got = f["chunked"][()]
+        assert got.dtype == np.int16 and np.array_equal(got, c)
+        assert f["chunked"].chunks == (4,) and f["chunked"].compression == "gzip"
