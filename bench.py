@@ -23,7 +23,8 @@ the 192^3 cylinder acquisition: all 256 shots, nt=2000), ring2d (the 2D 256^2
 ring, all 64 shots per launch), gn3d (the 224^3 Gauss-Newton Hessian-vector product),
 grad3d_large (320^3, 512 shots, 8 per launch), tfm2d (the TFM image of a
 64 x 1500 x 64 FMC), invert2d (iterations of the device-resident inversion
-loop on the 2D ring).  --misfit gcn and --windows run the gradient workloads
+loop on the 2D ring), io (the Dataset HDF5 file of the 192^3 acquisition:
+save and load on the host cores, no GPU).  --misfit gcn and --windows run the gradient workloads
 with the GCN misfit and with P-arrival data windows.
 """
 
@@ -602,6 +603,55 @@ def bench_fmc(args, prob):
     print(json.dumps(line))
 
 
+IO_WORKLOAD = ("Dataset HDF5 file (dataset.py:112-174 layout) of the 192^3 cylinder acquisition: "
+               "256 x 2000 x 256 FP32 traces (524 MB), gzip level 4 as the reference writes "
+               "them; one step = save + load")
+
+
+def bench_io(args):
+    """--workload io: the portable Dataset file written and read by
+    openusct_gb300.dataset_io (no h5py) on the host cores."""
+    import tempfile
+    import numpy as np
+    from openusct_gb300 import dataset_io
+    from openusct_gb300.acquire import ArrayGeometry, Dataset
+    rng = np.random.default_rng(0)
+    n_tx, nt, n_rx = 256, 2000, 256
+    t = np.arange(nt)
+    # band-limited seeded traces (compressibility like recorded wavelets, not noise)
+    data = (np.sin(0.05 * t[None, :, None] + rng.uniform(0, 2 * np.pi, (n_tx, 1, n_rx))) *
+            np.exp(-((t[None, :, None] - 1000) / 400.0) ** 2) * 1e-3).astype(np.float32)
+    ds = Dataset(ArrayGeometry(rng.standard_normal((n_rx, 3)) * 0.01, 0.015, 1e6, "cylinder"),
+                 data, 1 / 4.0e-8, np.zeros(nt), 1e6, 1500.0, np.arange(n_tx), None, {})
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "acq.h5")
+        saves, loads = [], []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            dataset_io.save(ds, path)
+            t1 = time.perf_counter()
+            got = dataset_io.load(path)
+            t2 = time.perf_counter()
+            if i >= args.warmup:
+                saves.append(t1 - t0)
+                loads.append(t2 - t1)
+        assert np.array_equal(got.data, data)
+        size = os.path.getsize(path)
+    ts, tl = statistics.median(saves), statistics.median(loads)
+    mb = data.nbytes / 1e6
+    cores = os.cpu_count() or 1
+    line = {"metric": "Dataset file MB/s (save + load of the FP32 traces)",
+            "value": 2 * mb / (ts + tl), "unit": "MB/s", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * (ts + tl), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": IO_WORKLOAD, "file_mb": size / 1e6, "cores": cores},
+            "save_mb_per_s": mb / ts, "load_mb_per_s": mb / tl,
+            "e2e": {"value": 2 * mb / (ts + tl), "unit": "MB/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0, "api": "openusct_gb300.dataset_io.save/load"},
+            "cpu_baseline": None, "gpu_launches": 0}
+    print(json.dumps(line))
+
+
 INVERT_WORKLOAD = ("FWI inversion loop (fwi.invert: steepest descent on the Gaussian-smoothed "
                    "gradient, backtracking line search), 2D 256^2 ring, dx=0.15mm, 64 elements, "
                    "two seeded discs, nt=1500, L2, model and gradient kept on the GPU")
@@ -800,7 +850,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="grad3d",
-                    choices=sorted(WORKLOADS) + ["fmc3d", "tfm2d", "invert2d"])
+                    choices=sorted(WORKLOADS) + ["fmc3d", "tfm2d", "invert2d", "io"])
     ap.add_argument("--n", type=int, default=0, help="override the grid size (smaller variants)")
     ap.add_argument("--nt", type=int, default=0, help="override the time levels")
     ap.add_argument("--batch", type=int, default=0)
@@ -828,6 +878,15 @@ def main():
         (bench_tfm if args.workload == "tfm2d" else bench_invert)(args)
         return
 
+    if args.workload == "io":
+        if rank != 0:
+            return
+        if args.impl == "reference":   # Dataset.save/load need h5py, absent here
+            print(json.dumps({"impl": "reference", "unavailable": "the reference's Dataset.save/"
+                              "load need h5py, which is not installed on this machine"}))
+            return
+        bench_io(args)
+        return
     if args.workload == "fmc3d":
         if rank != 0:
             return
