@@ -16,7 +16,6 @@ Tiles are written tile_x x tile_y [x zchunk [x variant [x stages]]].
 from __future__ import annotations
 
 import argparse
-import ctypes
 import json
 import os
 import threading

@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 import oracle
-from golden_util import CASES, grad_tol, load, rel_l2, rel_max, trace_tol
+from golden_util import CASES, grad_tol, load, rel_l2, trace_tol
 
 pytestmark = pytest.mark.gpu
 
