@@ -133,10 +133,13 @@ int usct_plan_check(usct_plan* plan, void* stream);
  * at a time on one model).  Shots of several forward requests on different
  * models of the same grid, h, dt, nt and wavelet share one plan, so they
  * advance in one launch: transmit t uses model model_of_tx[t] (host array of
- * n_tx entries, each < n_models).  Needs the TMA variant, >= 4 shot channels,
- * one level per launch, no sponge; forward sweeps only (USCT_MODE_FORWARD).
- * Call before the plan's first sweep: it grows usct_model_bytes by one
- * wavefield level per batch (S in the wavefields' layout). */
+ * n_tx entries, each < n_models), and each group of four transmits
+ * (4k .. 4k+3) must share one model (pad a request with transmits that have no
+ * source entries to keep the groups whole).  Needs the TMA variant, >= 4 shot
+ * channels, one level per launch, no sponge; forward sweeps only
+ * (USCT_MODE_FORWARD).  Call before the plan's first sweep: it grows
+ * usct_model_bytes by a quarter wavefield level per batch (S once per four
+ * channels). */
 int usct_plan_set_channel_models(usct_plan* plan, int n_models, const int* model_of_tx);
 /* The per-channel model S from n_models device FP64 models [n_models][cells]
  * and the FP64 wavelet, for a plan with per-channel models. */

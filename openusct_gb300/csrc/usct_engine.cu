@@ -425,8 +425,13 @@ extern "C" int usct_plan_info(const usct_plan* p, int key, int64_t* value) {
 // ---------------------------------------------------------------------------
 struct ModelWS {
     float* S; float* sp; float* vm; float* wav; double* g;
-    float* Spc;   // per-channel models: S of every batch in the wavefields' layout
+    float* Spc;   // per-channel models: S of every batch, one value per four channels
 };
+
+// floats of one batch's per-channel S ([z][y][x][C/4], 256-byte aligned)
+static size_t spc_floats(const usct_plan* p) {
+    return al256(p->LV / 4 * sizeof(float)) / sizeof(float);
+}
 static const int JBLK = 64;   // gather blocks (per-block FP64 misfit partials)
 
 static ModelWS carve_model(const usct_plan* p, void* base) {
@@ -446,7 +451,7 @@ extern "C" size_t usct_model_bytes(const usct_plan* p) {
     if (!p) return 0;
     return 3 * al256(p->cells_p * sizeof(float)) + al256((size_t)p->nt * sizeof(float)) +
            al256(p->cells_p * sizeof(double)) +
-           (p->pcs ? (size_t)p->nbatch * al256(p->LV * sizeof(float)) : 0);
+           (p->pcs ? (size_t)p->nbatch * spc_floats(p) * sizeof(float) : 0);
 }
 
 struct BatchWS {
@@ -517,18 +522,19 @@ __global__ void k_prepare(const double* __restrict__ m, const double* __restrict
     }
 }
 
-// S of every batch in the wavefields' layout [b][z][y][x][c] from per-transmit
-// models: transmit t = b*C + c uses models[tx_model[t]]; channels past the last
+// One batch's S, [z][y][x][C/4], from per-transmit models: quad q of a cell
+// holds channels 4q .. 4q+3, which share one model (usct_plan_set_channel_models
+// checks it), so it takes the model of transmit 4q; quads past the batch's last
 // transmit and padded cells get 0 (their fields stay 0).
 __global__ void k_prepare_channels(const double* __restrict__ models, const int* __restrict__ tx_model,
                                    float* Spc, double dt2, int nx, int nxs, int C, int logC,
                                    int n_tx, long long ncp, long long total) {
+    const int Q = C >> 2;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
          i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i & (C - 1));
-        const long long rest = i >> logC;           // (b, cell)
-        const long long cell = rest % ncp;
-        const int t = (int)(rest / ncp) * C + c;
+        const int q = (int)(i & (Q - 1));
+        const long long cell = i >> (logC - 2);
+        const int t = 4 * q;
         const int x = (int)(cell % nxs);
         float v = 0.f;
         if (t < n_tx && x < nx) {
@@ -728,7 +734,8 @@ static size_t stencil_smem(const usct_plan* p, int nfield) {
 
 // ---- tensor maps for the TMA ring -------------------------------------------
 enum MapKind { MK_WF_HALO = 0, MK_WF_OWN = 1, MK_CELL_OWN = 2, MK_CELL_HALO = 3, MK_G_OWN = 4,
-               MK2_A = 5, MK2_B = 6, MK2_S = 7 };   // MK2_*: the two-step tiles
+               MK2_A = 5, MK2_B = 6, MK2_S = 7,   // MK2_*: the two-step tiles
+               MK_QUAD_OWN = 8 };                 // per-channel models: one S per 4 channels
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -747,7 +754,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 // Box shapes (innermost first).  Wavefields: 4D {C, nxs, ny, nz} when C >= 4,
 // otherwise 3D {RP, ny, nz}; model cells: 3D {nxs, ny, nz} (float or double).
 static int get_map(usct_plan* p, const void* ptr, int kind, CUtensorMap* out) {
-    const uint64_t key = (uint64_t)(uintptr_t)ptr * 8u + (uint64_t)kind;
+    const uint64_t key = (uint64_t)(uintptr_t)ptr * 16u + (uint64_t)kind;
     auto it = p->maps.find(key);
     if (it != p->maps.end()) { *out = it->second; return USCT_OK; }
     auto enc = encode_fn();
@@ -774,6 +781,11 @@ static int get_map(usct_plan* p, const void* ptr, int kind, CUtensorMap* out) {
         dims[0] = g.nxs; dims[1] = g.ny; dims[2] = g.nz;
         strides[0] = (cuuint64_t)g.nxs * 4; strides[1] = (cuuint64_t)g.CPP * 4;
         box[0] = p->w2 + 8; box[1] = p->h2 + 2; box[2] = 1;
+    } else if (kind == MK_QUAD_OWN) {
+        // [z][y][x][C/4]: a row of RP / 4 floats; the own box is one quad per lane
+        dims[0] = (cuuint64_t)g.RP / 4; dims[1] = g.ny; dims[2] = g.nz;
+        strides[0] = (cuuint64_t)g.RP; strides[1] = (cuuint64_t)g.PP;   // bytes: RP/4 and PP/4 floats
+        box[0] = p->txv; box[1] = p->ty; box[2] = 1;
     } else if (kind == MK_WF_HALO || kind == MK_WF_OWN) {
         if (g.C >= 4) {
             rank = 4;
@@ -874,14 +886,17 @@ static int launch_fwd_tma(usct_plan* p, const FwdArgs& a0, cudaStream_t s) {
     const bool pcs = p->pcs && !BORN;
     TRY(get_map(p, a.pc, MK_WF_HALO, &mp.pc));
     TRY(get_map(p, a.pp, MK_WF_OWN, &mp.pp));
-    TRY(get_map(p, a.S, pcs ? MK_WF_OWN : MK_CELL_OWN, &mp.S));
+    TRY(get_map(p, a.S, pcs ? MK_QUAD_OWN : MK_CELL_OWN, &mp.S));
     if (a.sp) TRY(get_map(p, a.sp, MK_CELL_OWN, &mp.sp));
     if (BORN) {
         TRY(get_map(p, a.dc, MK_WF_HALO, &mp.dc));
         TRY(get_map(p, a.dpp, MK_WF_OWN, &mp.dpp));
         TRY(get_map(p, a.vm, MK_CELL_OWN, &mp.vm));
     }
-    const int R = BORN ? p->stages_born : p->stages_fwd;
+    // per-channel models add a quad row of S to every stage: six 3D stages of
+    // the 64x4 / 32-shot tile would no longer let three CTAs share an SM, five do
+    const int R = BORN ? p->stages_born
+                       : (pcs && p->ndim == 3 ? std::min(p->stages_fwd, 5) : p->stages_fwd);
     const FwdStage L = fwd_stage(p->txv, p->ty, p->ndim == 3, BORN, p->C, p->logC, a.sp != nullptr,
                                  pcs);
     const size_t smem = (size_t)R * L.floats * sizeof(float) + (size_t)R * 8 + 16;
@@ -1227,10 +1242,14 @@ extern "C" int usct_plan_set_channel_models(usct_plan* p, int n_models, const in
     if (p->variant != 1 || p->C < 4 || p->tb)
         return set_err(USCT_ERR_ARG, "per-channel models need the TMA variant, >= 4 shot channels "
                                      "and one level per launch");
-    for (int t = 0; t < p->n_tx; ++t)
+    for (int t = 0; t < p->n_tx; ++t) {
         if (model_of_tx[t] < 0 || model_of_tx[t] >= n_models)
             return set_err(USCT_ERR_ARG, "transmit %d names model %d of %d", t, model_of_tx[t],
                            n_models);
+        if (model_of_tx[t] != model_of_tx[t & ~3])
+            return set_err(USCT_ERR_ARG, "transmits %d..%d have different models: the model must "
+                           "be constant over each group of four transmits", t & ~3, t);
+    }
     cudaFree(p->d_tx_model);
     p->d_tx_model = nullptr;
     TRY(upload(&p->d_tx_model, std::vector<int>(model_of_tx, model_of_tx + p->n_tx)));
@@ -1247,13 +1266,13 @@ extern "C" int usct_model_prepare_channels(usct_plan* p, void* model_ws, const d
     if (!p->pcs) return set_err(USCT_ERR_STATE, "the plan has no per-channel models");
     cudaStream_t s = (cudaStream_t)stream;
     ModelWS M = carve_model(p, model_ws);
-    const long long lvf = (long long)(al256(p->LV * sizeof(float)) / sizeof(float));
-    // batch b's S starts at b * lvf (a level each, 256-byte aligned)
+    const size_t spf = spc_floats(p);
+    // batch b's S starts at b * spf
     for (int b = 0; b < p->nbatch; ++b) {
-        k_prepare_channels<<<grid1d((long long)p->LV), 256, 0, s>>>(
-            models, p->d_tx_model + (size_t)b * p->C, M.Spc + (size_t)b * lvf, p->dt * p->dt,
+        k_prepare_channels<<<grid1d((long long)p->LV / 4), 256, 0, s>>>(
+            models, p->d_tx_model + (size_t)b * p->C, M.Spc + (size_t)b * spf, p->dt * p->dt,
             p->geo.nx, p->geo.nxs, p->C, p->logC, std::min(p->C, p->n_tx - b * p->C),
-            (long long)p->cells_p, (long long)p->LV);
+            (long long)p->cells_p, (long long)p->LV / 4);
         ++p->launches;
     }
     k_wavelet<<<(p->nt + 255) / 256, 256, 0, s>>>(wavelet, M.wav, p->nt);
@@ -1433,7 +1452,7 @@ static int batch_forward_impl(usct_plan* p, const void* model_ws, void* batch_ws
         return gather(p, B, b, traces, nullptr, 0, s);
     }
     const size_t lvf = lvb / sizeof(float);
-    const float* Sb = p->pcs ? M.Spc + (size_t)b * lvf : M.S;   // this batch's S
+    const float* Sb = p->pcs ? M.Spc + (size_t)b * spc_floats(p) : M.S;   // this batch's S
     const int k = p->k, nt = p->nt;
     const int al = (p->nseg - 1) * k;
     for (int n = 1; n < nt; ++n) {

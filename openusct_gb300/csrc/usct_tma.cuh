@@ -52,7 +52,7 @@ __host__ __device__ constexpr int al32(int x) { return (x + 31) & ~31; }
 struct FwdStage {
     int o_pp, o_S, o_sp, o_dc, o_dpp, o_vm, floats;
 };
-// pcs: the model S is per shot channel (shot-innermost like the wavefields)
+// pcs: the model S per group of four shot channels (one value per lane)
 __host__ __device__ inline FwdStage fwd_stage(int TXV, int TY, bool is3d, bool born, int C, int logC,
                                               bool has_sp, bool pcs = false) {
     const int HF = C < 4 ? 4 : C;
@@ -63,7 +63,7 @@ __host__ __device__ inline FwdStage fwd_stage(int TXV, int TY, bool is3d, bool b
     FwdStage s{};
     s.o_pp = al32(rows * SR);
     s.o_S = s.o_pp + al32(TY * TXF);
-    s.o_sp = s.o_S + al32(TY * (pcs ? TXF : cells));
+    s.o_sp = s.o_S + al32(TY * (pcs ? TXF / 4 : cells));
     int end = s.o_sp + (has_sp ? al32(TY * cells) : 0);
     s.o_dc = end;
     if (born) {
@@ -317,9 +317,11 @@ static __device__ __noinline__ InjStep inject_residuals(float4 lk4, const RxEnt*
 // ---------------------------------------------------------------------------
 // forward step, TMA ring
 // ---------------------------------------------------------------------------
-// PCS: every shot channel has its own model (S in the wavefields' layout,
-// read as the own tile of a wavefield) -- the shots of co-admitted requests on
-// different models advancing in one launch; forward sweeps only, C >= 4.
+// PCS: the shot channels carry their own models -- the shots of co-admitted
+// requests on different models advancing in one launch; forward sweeps only,
+// C >= 4.  S is stored per group of four channels, [z][y][x][C/4]: a lane's
+// float4 holds four channels of one cell, so lane tx reads quad tx of the
+// tile row (C/4 floats per cell, where the wavefields hold C).
 template <int TXV, int TY, bool IS3D, bool BORN, int C, bool PCS = false>
 __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : ((TXV * TY >= 256) ? 4 : 8)) k_forward_tma(const FwdArgs a, const __grid_constant__ FwdMaps mp,
                                                          const int R, int* err) {
@@ -365,7 +367,7 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
     const float wv = a.wav[a.n - 1];
 
     const uint32_t b_halo = (uint32_t)(ROWS * SR * 4), b_own = (uint32_t)(TY * TXF * 4),
-                   b_cell = (uint32_t)(TY * cells * 4);
+                   b_cell = (uint32_t)(TY * cells * 4), b_quad = (uint32_t)(TY * TXV * 4);
     auto issue = [&](int i, int slot) {
         const int p = z0 - 1 + i;
         float* st = smf + (size_t)slot * L.floats;
@@ -373,7 +375,7 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         const bool inner = i >= 1 && i <= nloc - 2;
         uint32_t bytes = b_halo * (BORN ? 2u : 1u);
         if (inner)
-            bytes += b_own * (BORN ? 2u : 1u) + (PCS ? b_own : b_cell) +
+            bytes += b_own * (BORN ? 2u : 1u) + (PCS ? b_quad : b_cell) +
                      b_cell * ((has_sp ? 1u : 0u) + (BORN ? 1u : 0u));
         if (a.wait_test && i == 0) bytes += 16u;   // never delivered: exercises the bounded wait
         mbar_expect_tx(bar, bytes);
@@ -386,7 +388,7 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         if (inner) {
             if (C >= 4) tma4(st + L.o_pp, &mp.pp, bar, 0, x0c, y0, p);
             else tma3(st + L.o_pp, &mp.pp, bar, fx0, y0, p);
-            if (PCS) tma4(st + L.o_S, &mp.S, bar, 0, x0c, y0, p);
+            if (PCS) tma3(st + L.o_S, &mp.S, bar, fx0 >> 2, y0, p);   // quads: TXV a row
             else tma3(st + L.o_S, &mp.S, bar, x0c, y0, p);
             if (has_sp) tma3(st + L.o_sp, &mp.sp, bar, x0c, y0, p);
             if (BORN) {
@@ -450,7 +452,7 @@ __global__ void __launch_bounds__(TXV* TY, BORN ? ((TXV * TY >= 256) ? 2 : 4) : 
         const float4 cm = ld4(sm_m + r * SR + col);
         const float4 cp = ld4(sm_p + r * SR + col);
         const float4 ppv = ld4(sm_c + L.o_pp + ty * TXF + 4 * tx);
-        const float4 Sv = PCS ? ld4(sm_c + L.o_S + ty * TXF + 4 * tx)
+        const float4 Sv = PCS ? splat4(sm_c[L.o_S + ty * TXV + tx])
                               : cell4s(sm_c + L.o_S + ty * cells, 4 * tx, logC);
         const float4 spv = has_sp ? cell4s(sm_c + L.o_sp + ty * cells, 4 * tx, logC) : f4zero();
         const bool zy_in = y_in && z >= 1 && z <= g.nz - 2;

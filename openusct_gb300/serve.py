@@ -210,6 +210,17 @@ def _concat_csr(parts):
                np.concatenate([c.w for c in parts]))
 
 
+def _pad_rows(c, quantum):
+    """``c`` with empty rows (no entries) appended up to a multiple of
+    ``quantum`` rows: transmits that inject nothing, so their fields stay 0."""
+    from .geometry import CSR
+    extra = -c.rows % quantum
+    if not extra:
+        return c
+    ptr = np.concatenate([np.asarray(c.ptr, np.int32), np.full(extra, c.ptr[-1], np.int32)])
+    return CSR(ptr, c.cell, c.w)
+
+
 def _union_rows(parts):
     """One CSR holding each distinct row of several element CSR lists once (a
     row is its cells and weights), and per list the union row of each of its
@@ -238,6 +249,7 @@ class GpuExecutor:
     """Runs one request on the GB300 engine on its own stream."""
 
     merge_width = 32   # shots of one launch group (a batch)
+    merge_quantum = 4  # a request's shots fill whole groups of four channels (one model each)
 
     def __init__(self, device=None, graphs=False, workspace_bytes=None, merge=True):
         import torch
@@ -366,17 +378,20 @@ class GpuExecutor:
         from .geometry import element_csr
         shape = tuple(np.shape(reqs[0].m))
         parts = [element_csr(q.geom, shape, q.src_list, None) for q in reqs]
-        tx = _concat_csr([t for t, _ in parts])
+        padded = [_pad_rows(t, self.merge_quantum) for t, _ in parts]
+        tx = _concat_csr(padded)
         rx, rx_of = _union_rows([r for _, r in parts])
         C = self.merge_width
         q0 = reqs[0]
         plan = Plan(shape, q0.h, q0.dt, q0.nt, tx, rx, batch=C)
-        owner = np.concatenate([np.full(t.rows, i, np.int32) for i, (t, _) in enumerate(parts)])
+        owner = np.concatenate([np.full(t.rows, i, np.int32) for i, t in enumerate(padded)])
         _lib.check(plan._lib.usct_plan_set_channel_models(
             plan.handle, len(reqs), owner.ctypes.data_as(_lib._ip)))
         if not self.graphs:
             plan.set("graphs", 0)
-        plan.group_parts = [(t.rows, ix) for (t, _), ix in zip(parts, rx_of)]
+        # (first transmit, transmits, receiver columns) of each request
+        starts = np.cumsum([0] + [t.rows for t in padded[:-1]])
+        plan.group_parts = [(int(s), t.rows, ix) for s, (t, _), ix in zip(starts, parts, rx_of)]
         return plan
 
     def footprint_group(self, reqs, plan):
@@ -410,11 +425,8 @@ class GpuExecutor:
                                                   _lib.MODE_FORWARD, _ptr(data), s))
             plan.check(st)
             host = data.cpu().numpy()
-        out, t0 = [], 0
-        for nt_i, ix in plan.group_parts:
-            out.append({"traces": np.ascontiguousarray(host[t0:t0 + nt_i][:, :, ix])})
-            t0 += nt_i
-        return out
+        return [{"traces": np.ascontiguousarray(host[t0:t0 + n][:, :, ix])}
+                for t0, n, ix in plan.group_parts]
 
     def _gauss_newton(self, req, plan, m, w, sp, mws, st):
         """``n_iter`` Gauss-Newton iterations of the device-resident invert on
@@ -533,8 +545,13 @@ class Engine:
 
         i, rq = head
         width = getattr(self.ex, "merge_width", 32)
+        quantum = getattr(self.ex, "merge_quantum", 1)
+
+        def shots_of(q):   # channels a request takes in a group
+            return -(-q.n_shots // quantum) * quantum
+
         key = key_for(i, rq)
-        if key is None or rq.n_shots >= width:
+        if key is None or shots_of(rq) >= width:
             return None
         cands = [it for it in sorted(others, key=lambda it: (it[0], it[1]))
                  if not it[2].cancelled.is_set() and key_for(it[1], it[2]) == key]
@@ -542,15 +559,15 @@ class Engine:
         size = -(-(len(cands) + 1) // free)
         if size < 2:
             return None
-        group, shots = [head], rq.n_shots
+        group, shots = [head], shots_of(rq)
         for item in cands:
             if len(group) == size:
                 break
             j, oq = item[1], item[2]
-            if shots + oq.n_shots > width:
+            if shots + shots_of(oq) > width:
                 continue
             group.append((j, oq))
-            shots += oq.n_shots
+            shots += shots_of(oq)
         return group if len(group) > 1 else None
 
     # -- a whole stream ----------------------------------------------------------

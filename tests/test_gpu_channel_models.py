@@ -1,11 +1,13 @@
 """Shots on different models in one launch (usct_plan_set_channel_models).
 
 Forward requests of the same grid, spacing, time axis and wavelet share one
-plan whose shot channels each carry their own model.  The model operand is
-the same FP32 value per cell that the one-model plan broadcasts, so every
-request's traces must be bit-identical to its own plan's -- in 2D and 3D,
-with the group's transmits spread over several batches -- and a served group
-must give each request exactly what it gets when served alone.
+plan whose shot channels carry their own models, one per group of four
+channels (each request padded to whole groups with transmits that inject
+nothing).  The model operand is the same FP32 value per cell that the
+one-model plan broadcasts, so every request's traces must be bit-identical to
+its own plan's -- in 2D and 3D, with the group's transmits spread over several
+batches -- and a served group must give each request exactly what it gets
+when served alone.
 """
 
 import ctypes
@@ -33,13 +35,14 @@ def _group_traces(eng, models, geoms, src_lists, c, C):
     """Traces of several requests through one plan with per-channel models."""
     _lib, gb = eng
     from openusct_gb300.geometry import element_csr
-    from openusct_gb300.serve import _concat_csr, _union_rows
+    from openusct_gb300.serve import _concat_csr, _pad_rows, _union_rows
     shape = models[0].shape
     parts = [element_csr(g, shape, sl, None) for g, sl in zip(geoms, src_lists)]
-    tx = _concat_csr([t for t, _ in parts])
+    padded = [_pad_rows(t, 4) for t, _ in parts]
+    tx = _concat_csr(padded)
     rx, rx_of = _union_rows([r for _, r in parts])
     plan = gb.Plan(shape, c.h, c.dt, c.nt, tx, rx, batch=C)
-    owner = np.concatenate([np.full(t.rows, i, np.int32) for i, (t, _) in enumerate(parts)])
+    owner = np.concatenate([np.full(t.rows, i, np.int32) for i, t in enumerate(padded)])
     lib = _lib.load()
     _lib.check(lib.usct_plan_set_channel_models(plan.handle, len(models),
                                                 owner.ctypes.data_as(_lib._ip)))
@@ -58,9 +61,9 @@ def _group_traces(eng, models, geoms, src_lists, c, C):
     plan.check()
     host = d.cpu().numpy()
     out, t0 = [], 0
-    for (t, _), ix in zip(parts, rx_of):
+    for (t, _), tp, ix in zip(parts, padded, rx_of):
         out.append(host[t0:t0 + t.rows][:, :, ix])
-        t0 += t.rows
+        t0 += tp.rows
     plan.close()
     return out
 
@@ -99,6 +102,10 @@ def test_per_channel_models_are_refused_for_gradients(eng):
     bad = np.full(tx.rows, 3, np.int32)
     assert lib.usct_plan_set_channel_models(plan.handle, 2, bad.ctypes.data_as(_lib._ip)) \
         == _lib.USCT_ERR_ARG
+    mixed = np.zeros(tx.rows, np.int32)
+    mixed[5] = 1                      # transmits 4..7 would need two models
+    assert lib.usct_plan_set_channel_models(plan.handle, 2, mixed.ctypes.data_as(_lib._ip)) \
+        == _lib.USCT_ERR_ARG and b"group of four" in lib.usct_last_error()
     plan.close()
 
 

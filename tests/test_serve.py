@@ -250,6 +250,23 @@ def test_concatenated_element_lists():
     assert list(rx.ptr) == [0, 1, 2, 3, 4, 5] and rx.rows == 5 and len(rx.w) == 5
 
 
+def test_padded_transmit_rows_and_group_quantum():
+    from openusct_gb300.geometry import element_csr
+    from openusct_gb300.serve import _pad_rows
+    tx = element_csr([(1, 2), (3, 4), (5, 6)], (8, 8), [0, 2, 1, 0, 2])[0]
+    p = _pad_rows(tx, 4)
+    assert p.rows == 8 and list(p.ptr) == [0, 1, 2, 3, 4, 5, 5, 5, 5]
+    assert np.array_equal(p.cell, tx.cell) and _pad_rows(p, 4) is p
+    # with a quantum of 4, requests of 5 shots take 8 channels: 4 of them fill 32
+    ex = MergingExecutor()
+    ex.merge_quantum = 4
+    eng = Engine(ex, budget_bytes=10 ** 6, max_active=1)
+    reqs = [fwd(10, 0.05, 0.0, "a", shots=5) for _ in range(6)]
+    rs = eng.run_stream(reqs, realtime=False)
+    assert all(r.ok for r in rs)
+    assert max(len(g) for g in ex.groups) == 4
+
+
 def test_receiver_union_keeps_each_distinct_row_once():
     from openusct_gb300.geometry import element_csr
     from openusct_gb300.serve import _union_rows
