@@ -396,3 +396,44 @@ def test_reader_takes_structures_the_writer_does_not_emit(tmp_path):
         got = f["chunked"][()]
         assert got.dtype == np.int16 and np.array_equal(got, c)
         assert f["chunked"].chunks == (4,) and f["chunked"].compression == "gzip"
+
+
+def _library_file():
+    """A file the HDF5 library itself wrote: scipy's MATLAB 7.4 v7.3-format
+    test file (an HDF5 file behind a 512-byte user block)."""
+    try:
+        import scipy.io.matlab as sm
+    except ImportError:
+        return None
+    p = os.path.join(os.path.dirname(sm.__file__), "tests", "data", "testhdf5_7.4_GLNX86.mat")
+    return p if os.path.exists(p) else None
+
+
+@pytest.mark.skipif(_library_file() is None, reason="no HDF5 file written by the HDF5 library here")
+def test_a_file_the_hdf5_library_wrote():
+    """The reader takes a file written by the HDF5 library (user block,
+    superblock 0, symbol-table root, version-2 layout, fill-value,
+    modification-time and NIL messages), and the writer's FP64 datatype and
+    dataspace messages are byte-identical to the library's; its version-1
+    attribute message differs only in the fixed-length string padding
+    (null-padded, as h5py writes NumPy bytes, where the file is
+    null-terminated)."""
+    path = _library_file()
+    with hdf5.File(path, "r") as f:
+        assert f.keys() == ["testdouble"]
+        ds = f["testdouble"]
+        assert ds.shape == (9, 1) and ds.dtype == np.float64
+        assert np.allclose(ds[()][:, 0], np.arange(9) * np.pi / 4, rtol=1e-15, atol=0)
+        assert ds.attrs["MATLAB_class"] == b"double"
+    r = hdf5._Reader(path)
+    try:
+        msgs = {t: bytes(b) for t, b, _ in r.messages(r.links(r.root)["testdouble"])}
+        assert msgs[0x03] == hdf5._pad8(hdf5._dtype_message(np.dtype("<f8")))
+        assert msgs[0x01] == hdf5._space_message((9, 1))
+        ours = hdf5._pad8(hdf5._attr_message("MATLAB_class", b"double", None))
+        assert len(ours) == len(msgs[0x0C])
+        diff = [i for i in range(len(ours)) if ours[i] != msgs[0x0C][i]]
+        assert diff == [25]                  # the string datatype's padding-type bits
+        assert msgs[0x0C][25] == 0x00 and ours[25] == 0x01
+    finally:
+        r.close()
