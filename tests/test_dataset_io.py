@@ -3,11 +3,13 @@
 The round trips restate the reference's own tests (simulation/tests/
 test_dataset.py: 2D and 3D, ground truth kept; simulation/tests/
 test_uarp_format.py: data, geometry, timing and transmit map kept, and the
-UDSP group layout present).  No HDF5 implementation exists here to check the
-files against, so the format tests pin the structures themselves: the
+UDSP group layout present).  No HDF5 implementation exists here to read the
+files written here, so the format tests pin the structures themselves: the
 superblock, variable-length strings in a global heap, B-trees of several
 levels (small node ranks) and sibling links, chunked gzip data with an edge
-chunk, and a user block before the superblock.
+chunk, a user block before the superblock, a hand-built file of the
+structures newer writers use, and one file the HDF5 library itself wrote
+(read back, and its messages compared byte for byte with the writer's).
 """
 
 import os
