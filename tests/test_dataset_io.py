@@ -437,5 +437,21 @@ def test_a_file_the_hdf5_library_wrote():
         diff = [i for i in range(len(ours)) if ours[i] != msgs[0x0C][i]]
         assert diff == [25]                  # the string datatype's padding-type bits
         assert msgs[0x0C][25] == 0x00 and ours[25] == 0x01
+        # the group structures follow the conventions the writer uses: B-tree
+        # key 0 is the empty name (heap offset 0) and key 1 the child's last
+        # name; the heap starts with the empty string, names are 8-byte padded,
+        # and a free list ends with the offset the writer stores for "none"
+        stab = {t: bytes(b) for t, b, _ in r.messages(r.root)}[0x11]
+        bt, heap = (int.from_bytes(stab[i:i + 8], "little") + r.sb_base for i in (0, 8))
+        key0, child, key1 = struct.unpack("<QQQ", bytes(r.b[bt + 24:bt + 48]))
+        child += r.sb_base                    # file addresses are relative to the superblock
+        assert bytes(r.b[bt:bt + 4]) == b"TREE" and key0 == 0
+        assert bytes(r.b[child:child + 4]) == b"SNOD"
+        seg = r.addr(heap + 24)
+        assert bytes(r.b[seg:seg + 8]) == b"\0" * 8 and r._heap_name(heap, key1) == "testdouble"
+        assert key1 == 8 and r._heap_name(heap, 8) == "testdouble"
+        free = int.from_bytes(bytes(r.b[heap + 16:heap + 24]), "little")
+        assert int.from_bytes(bytes(r.b[seg + free:seg + free + 8]), "little") == \
+            hdf5._HEAP_FREE_NULL
     finally:
         r.close()
