@@ -297,3 +297,53 @@ def test_requests_are_grouped_only_when_they_outnumber_the_free_slots():
     # ceil(4/2) = 2 and ceil(2/1) = 2 -- every request admitted at once
     assert sorted(len(g) for g in ex.groups) == [2, 2, 3, 3]
     assert eng.max_concurrent == 4
+
+
+def test_launch_group_layout_pads_requests_to_whole_quads(monkeypatch):
+    """plan_for_group on the host: each request's transmits start on a group
+    of four channels (padded with transmits that inject nothing), the owner
+    map names one model per group, and each request's traces are cut from
+    its own first transmit and its receivers' columns of the union."""
+    import openusct_gb300.backend as gb
+    from openusct_gb300.geometry import IndexGeometry
+    from openusct_gb300.serve import GpuExecutor, Request
+    seen = {}
+
+    class FakeLib:
+        @staticmethod
+        def usct_plan_set_channel_models(handle, n, owner_ptr):
+            seen["models"] = (n, np.ctypeslib.as_array(owner_ptr, shape=(seen["tx"].rows,)).copy())
+            return 0
+
+    class FakePlan:
+        _lib = FakeLib()
+        handle = None
+
+        def __init__(self, shape, h, dt, nt, tx, rx, batch=None):
+            seen["tx"], seen["rx"], seen["batch"] = tx, rx, batch
+
+        def set(self, *a):
+            pass
+
+    monkeypatch.setattr(gb, "Plan", FakePlan)
+    ex = GpuExecutor.__new__(GpuExecutor)
+    ex.graphs = False
+    geom = IndexGeometry([(1, 1), (1, 6), (6, 1), (6, 6), (3, 4), (4, 3)])
+    other = IndexGeometry([(1, 1), (2, 5)])           # shares one element with geom
+    m = np.ones((8, 8))
+    reqs = [Request(kind="forward", m=m, geom=g, wavelet=np.zeros(4), dt=1.0, h=1.0, nt=4,
+                    src_list=sl) for g, sl in ((geom, [0, 1, 2, 3, 4]), (other, [0, 1]),
+                                               (geom, [5, 4, 3]))]
+    plan = ex.plan_for_group(reqs)
+    tx = seen["tx"]
+    assert tx.rows == 8 + 4 + 4 and seen["batch"] == 32
+    n, owner = seen["models"]
+    assert n == 3 and list(owner) == [0] * 8 + [1] * 4 + [2] * 4
+    assert all(owner[t] == owner[t & ~3] for t in range(tx.rows))
+    assert [p[:2] for p in plan.group_parts] == [(0, 5), (8, 2), (12, 3)]
+    rows = np.diff(tx.ptr)
+    assert list(rows) == [1] * 5 + [0] * 3 + [1] * 2 + [0] * 2 + [1] * 3 + [0]
+    assert seen["rx"].rows == 7                        # 6 + 1 new receiver
+    assert list(plan.group_parts[0][2]) == [0, 1, 2, 3, 4, 5]
+    assert list(plan.group_parts[1][2]) == [0, 6]
+    assert list(plan.group_parts[2][2]) == [0, 1, 2, 3, 4, 5]
