@@ -447,6 +447,13 @@ def _serialize(root, path, leaf_k=None, internal_k=16, workers=None):
 class _Reader:
     def __init__(self, path):
         self.f = open(path, "rb")
+        try:
+            self._open(path)
+        except BaseException:
+            self.f.close()
+            raise
+
+    def _open(self, path):
         size = os.fstat(self.f.fileno()).st_size
         self.mm = mmap.mmap(self.f.fileno(), 0, access=mmap.ACCESS_READ) if size else b""
         self.b = memoryview(self.mm) if size else memoryview(b"")

@@ -464,6 +464,7 @@ class Engine:
         self.budget = int(budget_bytes)
         self.max_active = int(max_active)
         self.lock = threading.Condition()
+        self._merge_keys = {}   # request index -> merge key (one run_stream)
         self.reserved = 0
         self.active = 0
         self.peak_reserved = 0
@@ -697,7 +698,10 @@ class Engine:
             # freeing device memory waits for the device: never under the lock,
             # so admission does not stall behind running sweeps
             for pl in drop:
-                self.ex.release(pl)
+                try:
+                    self.ex.release(pl)
+                except Exception:      # a plan that fails to close must not stop admission
+                    pass
             if finished:
                 break
         for th in threads:
